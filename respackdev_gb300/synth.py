@@ -1,0 +1,349 @@
+"""Seeded synthetic band-structure inputs in RESPACK's file formats.
+
+The reference ships no ``dir-wfn`` (it needs Quantum ESPRESSO / xTAPP runs), so
+every workload of this package is generated here from a seed and written in the
+exact formats the reference reads:
+
+* ``dir-wfn/dat.{bandcalc,lattice,symmetry,sample-k,nkm,eigenvalue,kg}`` as
+  list-directed text and ``dir-wfn/dat.wfn`` as a Fortran unformatted
+  sequential file (one ``ncomp`` record, then one record of ``NGI(k)``
+  complex(8) coefficients per (k, band)).  Writers follow
+  ``util/qe2respack/qe2respack.f90:118-272``; readers are
+  ``src/chiqw/chiqw.F:87-329`` and ``:1106-1158``.
+* ``dir-wan/dat.ns-nb``, ``dat.umat`` (list-directed complex ``(re,im)``),
+  ``dat.wan`` (unformatted: ``NWF`` then one record of ``NG0(k) x NWF``
+  complex(8) per full-mesh k) and ``dat.wan-center``; writers follow
+  ``src/wannier/wannier.F:567-572, 2127-2215``.
+
+Units follow the reference: lengths in bohr, band energies and the Fermi
+level in Hartree, the wave-function cutoff in Rydberg (|k+G|^2 in bohr^-2).
+The symmetry file lists the identity only, and the sample-k list holds the
+whole Gamma-centred mesh, so the reference's unfolding (time reversal
+included, ``chiqw.F:437-480``) reproduces the mesh.
+"""
+from __future__ import annotations
+
+import dataclasses
+import os
+import struct
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+AU_EV = 27.21151  # Hartree in eV, as src/chiqw/config.h:19
+TPI = 2.0 * np.pi
+
+
+@dataclasses.dataclass
+class SynthSpec:
+    """What to generate.  Energies are in eV here and written in Hartree."""
+
+    lattice: str = "fcc"          # fcc | bcc | sc
+    a: float = 10.26              # conventional lattice constant (bohr)
+    nk: Sequence[int] = (4, 4, 4)  # Gamma-centred Monkhorst-Pack mesh
+    nbands: int = 40
+    nocc: int = 8
+    ecut_psi: float = 16.0        # Ry
+    gap_ev: float = 1.0
+    top_ev: float = 40.0
+    occ_width_ev: float = 10.0    # spread of the occupied manifold
+    disp_ev: float = 0.6          # band dispersion amplitude
+    metal: bool = False           # Fermi level inside the lowest empty bands
+    seed: int = 1234
+    shuffle_g: bool = True        # write each PW list in a seeded order
+    # band-cRPA target window (1-based, inclusive) written to dir-wan
+    wan_lo: int = 9
+    wan_hi: int = 11
+    wan_mode: str = "identity"    # identity | random  (dat.umat)
+    nwf: int = 0                  # Wannier orbitals for calc_int (0 = none)
+    wan_sigma: float = 1.2        # Gaussian width of the synthetic orbitals (bohr)
+
+
+# ----------------------------------------------------------------------------
+# lattice and mesh
+# ----------------------------------------------------------------------------
+def lattice_vectors(kind: str, a: float) -> np.ndarray:
+    h = 0.5 * a
+    if kind == "fcc":
+        return np.array([[0, h, h], [h, 0, h], [h, h, 0]], dtype=np.float64)
+    if kind == "bcc":
+        return np.array([[-h, h, h], [h, -h, h], [h, h, -h]], dtype=np.float64)
+    if kind == "sc":
+        return np.eye(3) * a
+    raise ValueError(f"unknown lattice {kind!r}")
+
+
+def reciprocal(avec: np.ndarray):
+    a1, a2, a3 = avec
+    vol = float(np.dot(a1, np.cross(a2, a3)))
+    b1 = np.cross(a2, a3) * TPI / vol
+    b2 = np.cross(a3, a1) * TPI / vol
+    b3 = np.cross(a1, a2) * TPI / vol
+    return np.array([b1, b2, b3]), vol
+
+
+def fold_half(x: float) -> float:
+    """Map a fractional coordinate into (-1/2, 1/2]."""
+    y = x - np.floor(x + 0.5)
+    if y <= -0.5 + 1e-12:
+        y += 1.0
+    return float(y)
+
+
+def gamma_mesh(nk: Sequence[int]) -> np.ndarray:
+    n1, n2, n3 = nk
+    pts = []
+    for i3 in range(n3):
+        for i2 in range(n2):
+            for i1 in range(n1):
+                pts.append([fold_half(i1 / n1), fold_half(i2 / n2), fold_half(i3 / n3)])
+    return np.array(pts, dtype=np.float64)
+
+
+def sphere(bvec: np.ndarray, ecut: float, k: np.ndarray) -> np.ndarray:
+    """Integer G with |k+G|^2 <= ecut, in the triple-loop order of the
+    reference's ``make_KG0`` (``chiqw_sub.F:785-801``: first index outermost)."""
+    # n_i = (k+G).a_i/(2 pi) - k_i and |(k+G).a_i| <= sqrt(ecut)|a_i|
+    avec = TPI * np.linalg.inv(bvec).T
+    alen = np.linalg.norm(avec, axis=1)
+    nmax = (np.sqrt(ecut) * alen / TPI + np.abs(k) + 2).astype(int)
+    r = [np.arange(-nmax[i], nmax[i] + 1) for i in range(3)]
+    g1, g2, g3 = np.meshgrid(r[0], r[1], r[2], indexing="ij")
+    G = np.stack([g1.ravel(), g2.ravel(), g3.ravel()], axis=1)
+    kg = (G + k[None, :]) @ bvec
+    sel = np.einsum("ij,ij->i", kg, kg) <= ecut
+    return G[sel].astype(np.int64)
+
+
+# ----------------------------------------------------------------------------
+# band energies (eV) and coefficients
+# ----------------------------------------------------------------------------
+def band_energies(spec: SynthSpec, kpts: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+    """(nbands, nk) energies in eV with E_F = 0.
+
+    The occupied manifold is a seeded 8-orbital-style tight-binding model
+    (cosine dispersion on the three reciprocal axes), the empty bands are
+    spread uniformly up to ``top_ev`` with their own dispersion.  A gap of
+    ``gap_ev`` separates them unless ``metal`` is set, in which case the Fermi
+    level cuts through the lowest empty bands."""
+    nb, nocc = spec.nbands, spec.nocc
+    nk = kpts.shape[0]
+    cosk = np.cos(TPI * kpts)            # (nk, 3)
+    cos2 = np.cos(TPI * (kpts[:, [0]] + kpts[:, [1]] - kpts[:, [2]]))[:, 0]
+    E = np.zeros((nb, nk))
+    for n in range(nocc):
+        c = -spec.occ_width_ev + (spec.occ_width_ev - 1.0) * (n / max(nocc - 1, 1))
+        t = rng.uniform(0.2, 1.0, size=3) * spec.disp_ev / 3.0
+        t2 = rng.uniform(-0.3, 0.3) * spec.disp_ev / 3.0
+        E[n] = c + cosk @ t + t2 * cos2
+    nun = nb - nocc
+    for m in range(nun):
+        frac = m / max(nun - 1, 1)
+        c = frac * spec.top_ev
+        t = rng.uniform(0.2, 1.0, size=3) * spec.disp_ev
+        t2 = rng.uniform(-0.3, 0.3) * spec.disp_ev
+        E[nocc + m] = c + cosk @ t + t2 * cos2
+    vbm = E[:nocc].max()
+    E[:nocc] += -0.5 * spec.gap_ev - vbm
+    cbm = E[nocc:].min()
+    E[nocc:] += 0.5 * spec.gap_ev - cbm
+    if spec.metal:
+        # put E_F inside the first empty band: mid-way between its min and max
+        lo, hi = E[nocc].min(), E[nocc].max()
+        shift = 0.5 * (lo + hi)
+        E -= shift
+    return E
+
+
+def orthonormal_coeffs(npw: int, nb: int, rng: np.random.Generator) -> np.ndarray:
+    """Gram-Schmidt (QR) orthonormalised complex Gaussian columns (npw, nb)."""
+    z = rng.standard_normal((npw, nb)) + 1j * rng.standard_normal((npw, nb))
+    q, r = np.linalg.qr(z)
+    # fix the phase convention so the result is independent of the LAPACK sign choice
+    d = np.diag(r)
+    q = q * (d / np.abs(d))[None, :]
+    return np.ascontiguousarray(q)
+
+
+# ----------------------------------------------------------------------------
+# Fortran file helpers
+# ----------------------------------------------------------------------------
+def fmt_real(x: float) -> str:
+    return f"{x: .16E}"
+
+
+def write_unformatted_record(f, payload: bytes):
+    """One Fortran sequential unformatted record (4-byte markers, gfortran)."""
+    n = len(payload)
+    if n > 2147483639:
+        raise ValueError("records above 2 GiB are written by the C writer")
+    f.write(struct.pack("<i", n))
+    f.write(payload)
+    f.write(struct.pack("<i", n))
+
+
+def read_unformatted_records(path: str) -> List[bytes]:
+    out = []
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    while pos < len(data):
+        (n,) = struct.unpack_from("<i", data, pos)
+        cont = n < 0
+        n = abs(n)
+        chunk = data[pos + 4: pos + 4 + n]
+        pos += 8 + n
+        while cont:
+            (m,) = struct.unpack_from("<i", data, pos)
+            cont = m < 0
+            m = abs(m)
+            chunk += data[pos + 4: pos + 4 + m]
+            pos += 8 + m
+        out.append(chunk)
+    return out
+
+
+# ----------------------------------------------------------------------------
+# main generator
+# ----------------------------------------------------------------------------
+@dataclasses.dataclass
+class SynthData:
+    avec: np.ndarray
+    bvec: np.ndarray
+    volume: float
+    kpts: np.ndarray           # (nk, 3) fractional
+    kg: List[np.ndarray]       # per k: (npw_k, 3) int
+    coeffs: List[np.ndarray]   # per k: (npw_k, nbands) complex
+    energies: np.ndarray       # (nbands, nk) Hartree
+    efermi: float              # Hartree
+    ecut_psi: float            # Ry
+
+
+def generate(spec: SynthSpec) -> SynthData:
+    rng = np.random.default_rng(spec.seed)
+    avec = lattice_vectors(spec.lattice, spec.a)
+    bvec, vol = reciprocal(avec)
+    kpts = gamma_mesh(spec.nk)
+    Eev = band_energies(spec, kpts, rng)
+    kg, coeffs = [], []
+    for ik in range(kpts.shape[0]):
+        G = sphere(bvec, spec.ecut_psi, kpts[ik])
+        if spec.shuffle_g:
+            G = G[rng.permutation(G.shape[0])]
+        kg.append(G)
+        coeffs.append(orthonormal_coeffs(G.shape[0], spec.nbands, rng))
+    return SynthData(avec=avec, bvec=bvec, volume=vol, kpts=kpts, kg=kg, coeffs=coeffs,
+                     energies=Eev / AU_EV, efermi=0.0, ecut_psi=spec.ecut_psi)
+
+
+def write_dir_wfn(root: str, d: SynthData, ncomp: int = 1):
+    w = os.path.join(root, "dir-wfn")
+    os.makedirs(w, exist_ok=True)
+    nk = d.kpts.shape[0]
+    nb = d.energies.shape[0]
+    with open(os.path.join(w, "dat.bandcalc"), "w") as f:
+        f.write(fmt_real(d.ecut_psi) + "\n")
+        f.write(fmt_real(d.efermi) + "\n")
+        f.write(fmt_real(0.0) + "\n")
+    with open(os.path.join(w, "dat.lattice"), "w") as f:
+        for v in d.avec:
+            f.write(" ".join(fmt_real(x) for x in v) + "\n")
+    with open(os.path.join(w, "dat.symmetry"), "w") as f:
+        f.write("%5d\n%5d\n" % (1, 1))
+        f.write("".join("%3d" % v for v in (1, 0, 0, 0, 1, 0, 0, 0, 1)) + "\n")
+        f.write("%3d%3d%3d\n" % (0, 0, 0))
+    with open(os.path.join(w, "dat.sample-k"), "w") as f:
+        f.write("%12d\n" % nk)
+        for k in d.kpts:
+            f.write(" ".join(fmt_real(x) for x in k) + "\n")
+    with open(os.path.join(w, "dat.nkm"), "w") as f:
+        for G in d.kg:
+            f.write("%12d\n" % G.shape[0])
+    with open(os.path.join(w, "dat.kg"), "w") as f:
+        for G in d.kg:
+            f.write("%12d\n" % G.shape[0])
+            for g in G:
+                f.write("%12d%12d%12d\n" % tuple(int(x) for x in g))
+    with open(os.path.join(w, "dat.eigenvalue"), "w") as f:
+        f.write("%12d\n" % nb)
+        for ik in range(nk):
+            for ib in range(nb):
+                f.write(fmt_real(d.energies[ib, ik]) + "\n")
+    with open(os.path.join(w, "dat.wfn"), "wb") as f:
+        write_unformatted_record(f, struct.pack("<i", ncomp))
+        for ik in range(nk):
+            c = d.coeffs[ik]
+            for ib in range(nb):
+                write_unformatted_record(f, np.ascontiguousarray(c[:, ib]).astype("<c16").tobytes())
+
+
+def write_dir_wan(root: str, spec: SynthSpec, d: SynthData, full_kg: Optional[List[np.ndarray]] = None,
+                  full_k: Optional[np.ndarray] = None):
+    """Band-cRPA target window (dat.ns-nb, dat.umat) and, when ``spec.nwf`` is
+    set, synthetic Gaussian Wannier orbitals (dat.wan, dat.wan-center) on the
+    full-mesh plane-wave lists ``full_kg`` (the lists the reference rebuilds
+    with ``make_KG0``)."""
+    w = os.path.join(root, "dir-wan")
+    os.makedirs(w, exist_ok=True)
+    rng = np.random.default_rng(spec.seed + 7)
+    nk = d.kpts.shape[0]
+    nwin = spec.wan_hi - spec.wan_lo + 1
+    with open(os.path.join(w, "dat.ns-nb"), "w") as f:
+        for _ in range(nk):
+            f.write("%12d%12d\n" % (spec.wan_lo - 1, nwin))
+    with open(os.path.join(w, "dat.umat"), "w") as f:
+        f.write("%12d\n" % nwin)
+        for _ in range(nk):
+            if spec.wan_mode == "identity":
+                U = np.eye(nwin, dtype=np.complex128)
+            else:
+                z = rng.standard_normal((nwin, nwin)) + 1j * rng.standard_normal((nwin, nwin))
+                q, _ = np.linalg.qr(z)
+                U = q * rng.uniform(0.6, 1.0, size=(nwin, 1))  # partial weight
+            for ib in range(nwin):
+                f.write(" ".join("(%s,%s)" % (fmt_real(U[ib, jw].real).strip(), fmt_real(U[ib, jw].imag).strip())
+                                 for jw in range(nwin)) + "\n")
+    if spec.nwf > 0:
+        assert full_kg is not None and full_k is not None
+        centers = rng.uniform(0.0, 1.0, size=(spec.nwf, 3)) @ d.avec
+        with open(os.path.join(w, "dat.wan-center"), "w") as f:
+            f.write("#Wannier center\n#1:x, 2:y, 3:z (in xyz coord)\n")
+            for c in centers:
+                f.write("".join("%20.10f" % x for x in c) + "\n")
+        with open(os.path.join(w, "dat.wan"), "wb") as f:
+            write_unformatted_record(f, struct.pack("<i", spec.nwf))
+            for ik in range(full_k.shape[0]):
+                G = full_kg[ik]
+                kG = (G + full_k[ik][None, :]) @ d.bvec
+                k2 = np.einsum("ij,ij->i", kG, kG)
+                cols = []
+                for iw in range(spec.nwf):
+                    sig = spec.wan_sigma * (1.0 + 0.15 * iw)
+                    c = np.exp(-0.5 * sig * sig * k2) * np.exp(-1j * (kG @ centers[iw]))
+                    c /= np.linalg.norm(c)
+                    cols.append(c)
+                C = np.stack(cols, axis=1)  # (NG0, NWF), column-major record
+                write_unformatted_record(f, np.asfortranarray(C).T.ravel().astype("<c16").tobytes())
+
+
+def make_case(root: str, spec: SynthSpec, with_wan: bool = True) -> SynthData:
+    d = generate(spec)
+    write_dir_wfn(root, d)
+    if with_wan:
+        write_dir_wan(root, spec, d)
+    return d
+
+
+# Named synthetic cases used by the tests, the smoke check and the bench.
+CASES = {
+    # two-by-two-by-two mesh, small basis: the quick parity case
+    "tiny": SynthSpec(nk=(2, 2, 2), nbands=12, nocc=4, ecut_psi=8.0, seed=11,
+                      wan_lo=5, wan_hi=7),
+    "tiny_metal": SynthSpec(nk=(2, 2, 2), nbands=12, nocc=4, ecut_psi=8.0, seed=12,
+                            metal=True, wan_lo=5, wan_hi=7, wan_mode="random"),
+    # odd mesh exercises the odd branch of make_index_kpt
+    "tiny_odd": SynthSpec(nk=(3, 3, 3), nbands=10, nocc=4, ecut_psi=6.0, seed=13,
+                          wan_lo=5, wan_hi=6),
+    # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
+    "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
+}
