@@ -1,0 +1,133 @@
+/*
+ * respack_gb300.h -- C ABI of the GB300 (sm_103a) cRPA polarization library.
+ *
+ * Drop-in for RESPACK's chiqw path (src/chiqw).  RESPACK has no plugin or FFI
+ * layer; its boundaries are the calc_chiqw executable (stdin namelist +
+ * dir-wfn/dir-wan in, dir-eps out) and the subroutine seam inside the q loop of
+ * src/chiqw/chiqw.F.  Each entry point below names the reference code it
+ * replaces.  All arrays are caller-owned host memory, column-major (Fortran
+ * order), complex numbers as interleaved (re, im) doubles.  Every call returns
+ * 0 on success, >0 for an input error and <0 for a device error; the message is
+ * available from rp_last_error().  One context owns one CUDA stream; calls on a
+ * context must not overlap.
+ */
+#ifndef RESPACK_GB300_H
+#define RESPACK_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arithmetic of the chi0 contraction (the rest of the path is fixed:
+ * FP64 tetrahedron weights, FP64 eps and its inversion). */
+enum rp_precision {
+  RP_PREC_FP64 = 0,    /* plain FP64 everywhere (pair densities, contraction)      */
+  RP_PREC_FP16X2 = 1,  /* FP32 pair densities; tcgen05 contraction, 2-term FP16
+                          split (3 products), FP32 accumulate, FP64 chunk reduce  */
+  RP_PREC_BF16X3 = 2   /* as FP16X2 with a 3-term BF16 split (6 products)        */
+};
+
+/* &param_chiqw (src/chiqw/m_rdinput.f90:41-45, defaults :52-73) in the
+ * namelist's units (eV, Ry), plus extensions (&param_gpu). */
+typedef struct rp_params {
+  int    n_calc_band;
+  double ecut_for_eps;
+  double shift_ef;
+  double max_excitation_energy;
+  double green_func_delt;
+  double ttrhdrn_dmna;
+  double ttrhdrn_dmnr;
+  int    num_freq_grid;
+  double lower_bound_energy_window;
+  double upper_bound_energy_window;
+  int    flg_crpa;
+  int    flg_calc_type;
+  int    file_num_log_start;
+  int    file_num_eps_start;
+  int    file_num_eps_base_start;
+  int    n_calc_q;
+  int    mpi_num_qcomm;        /* q communities: here the number of q shards */
+  /* --- &param_gpu extensions --- */
+  int    precision;            /* enum rp_precision                          */
+  int    fft_box[3];           /* 0 0 0: reference rule (chiqw.F:389-401)    */
+  int    dump_chi;             /* also write dir-eps/qNNN/dat.chi0           */
+  int    device;               /* CUDA device ordinal                        */
+  int    max_pairs;            /* >0: keep only the first pairs (timing)     */
+  int    qshard_index;         /* this process's shard of the q list        */
+  int    qshard_count;         /* number of shards (1 = all q here)          */
+} rp_params;
+
+/* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */
+void rp_default_params(rp_params *p);
+
+/* Parse a namelist text holding &param_chiqw (and optionally the q index list
+ * that follows it, m_rdinput.f90:97-103, and &param_gpu).  qlist receives up to
+ * qcap indices, em up to emcap explicit frequencies (complex, Hartree).
+ * Replaces read_input (m_rdinput.f90:47-129). */
+int rp_parse_namelist(const char *text, rp_params *p, int *qlist, int qcap, int *nq,
+                      double *em, int emcap, int *nen_explicit);
+
+typedef struct rp_ctx rp_ctx;
+
+/* Size/geometry report of a context. */
+typedef struct rp_info {
+  int ntk, nk_irr, nkb[3], ntg, ntb, ncb, nen;
+  int n_occ, n_vir, n_docc, n_pocc, n_uocc;
+  int fft_box[3];
+  double volume, efermi, ecut_psi, ecut_eps;
+  double device_bytes;         /* HBM held by the context */
+} rp_info;
+
+/* Build a context from a run directory holding dir-wfn (and dir-wan for
+ * band-cRPA): reads the files like chiqw.F:87-329 and :870-906, unfolds the
+ * Brillouin zone (:419-545), classifies bands (:817-967), makes the frequency
+ * grid (:1184-1192, or the explicit grid em/nen_explicit when nen_explicit>0),
+ * uploads the wave functions and computes their real-space periodic parts on
+ * the device once (the reference recomputes them for every band pair,
+ * chiqw_sub.F:128-163). */
+int rp_ctx_create(rp_ctx **out, const char *root, const rp_params *p, const double *em,
+                  int nen_explicit);
+
+int rp_ctx_info(const rp_ctx *ctx, rp_info *info);
+
+/* Number of entries of dat.sample-k (= candidate q points). */
+int rp_num_qirr(const rp_ctx *ctx);
+
+/* chi0(G,G',w) of irreducible point iq (1-based index of dat.sample-k), after
+ * /VOLUME and before the spin factor: the array chiqw of chiqw.F:1476 (q != 0,
+ * layout (ng, ng, nen)) or chiqwgm of :1989 (Gamma, (ng, ng, nen, 3)).
+ * Replaces the pair loop chiqw.F:1264-1472 (q != 0) and :1578-1985 (Gamma):
+ * pair densities (calc_InterStateMatrix), tetrahedron weights (ttrhdrn_chi0)
+ * and the contraction.  chi may be NULL (result stays on the device for
+ * rp_epsinv_q).  ng_out / ndir_out report the sizes. */
+int rp_chi0_q(rp_ctx *ctx, int iq, double *chi, int *ng_out, int *ndir_out);
+
+/* eps^-1(G,G',w) of the last rp_chi0_q: calc_eps_rpa / calc_eps_rpa_q_0 and
+ * invZGE (chiqw_sub.F:386-568, invZGE.F90:1-22), FP64 on the device.
+ * Layout as chi.  epsinv may be NULL. */
+int rp_epsinv_q(rp_ctx *ctx, double *epsinv);
+
+/* Write dir-eps/qNNN for the last rp_chi0_q/rp_epsinv_q: dat.sq,
+ * dat.epsqw.600(-602), dat.epsqw.6NN0MM text diagonals and dat.log.400 last
+ * (chiqw.F:1493-1548, :2012-2076). */
+int rp_write_q(rp_ctx *ctx, const char *root);
+
+/* Whole calc_chiqw run (PROGRAM DIELECTRIC, chiqw.F:1-2100) in directory
+ * root with the namelist text (stdin content of the reference). */
+int rp_calc_chiqw(const char *root, const char *namelist_text);
+
+/* Seconds spent in each stage of the last rp_chi0_q + rp_epsinv_q (device
+ * time from CUDA events): [0] tetrahedron weights, [1] pair densities,
+ * [2] contraction, [3] eps build + inversion, [4] total chi0_q. */
+int rp_stage_times(const rp_ctx *ctx, double *t5);
+
+/* Number of kernel launches issued by this context so far. */
+long long rp_kernel_launches(const rp_ctx *ctx);
+
+const char *rp_last_error(const rp_ctx *ctx);
+void rp_ctx_destroy(rp_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,562 @@
+// rp_ctx.cpp -- the context behind the C ABI (include/respack_gb300.h).
+//
+// A context owns one CUDA stream and the device-resident data of a run: the
+// irreducible wave-function coefficients, the unfolding map, and -- computed
+// once -- the full-mesh coefficients and their real-space periodic parts.  Per
+// q point it uploads the small task tables (G sphere, k+q map, band pairs) and
+// runs, in band-pair batches sized for HBM:
+//   tetrahedron weights -> pair densities -> contraction (FP64 or tensor-core)
+// then the dielectric matrix build and inversion.  Results stay on the device
+// until the caller asks for a host copy or the dir-eps files.
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "rp_dev.cuh"
+#include "rp_host.h"
+#include "rp_tc.h"
+
+namespace {
+
+using rp::cd;
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  void ensure(size_t n) {
+    if (n <= bytes) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (n == 0) return;
+    RP_CUDA(cudaMalloc(&p, n));
+    bytes = n;
+  }
+  template <typename T> T *as() const { return (T *)p; }
+  void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
+};
+
+template <typename T> void upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
+  b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16));
+  if (!v.empty()) RP_CUDA(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+}
+
+}  // namespace
+
+struct rp_ctx {
+  rp::Setup S;
+  rp::UnfoldMap U;
+  std::string root;
+  int dev = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  long long launches = 0;
+  int R[3]{};  // psi-sphere extent per dimension
+  // persistent device data
+  DevBuf coef, numirr, trs, src, phase, ng0, kg0, cfull, ur, energy, prob, imt1, index2, em, b9, sk0, errw;
+  // per-q device data
+  DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
+      rowcol, A, eps, prow, fcol, piv, used, intra, pwpl;
+  rp::TcWorkspace tcw;
+  rp::QTask task;
+  int ndir = 1;
+  double wd[3]{};
+  bool have_chi = false, have_eps = false;
+  std::vector<cd> h_chi, h_eps;
+  cudaEvent_t ev[6]{};
+  double times[5]{};
+  ~rp_ctx() {
+    for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
+                      &b9, &sk0, &errw, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
+                      &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
+                      &intra, &pwpl})
+      b->release();
+    tcw.release();
+    for (auto &e : ev) if (e) cudaEventDestroy(e);
+    if (st) cudaStreamDestroy(st);
+  }
+};
+
+static thread_local std::string g_create_err;
+
+template <typename F> static int guarded(rp_ctx *ctx, F &&f) {
+  try {
+    f();
+    return 0;
+  } catch (const rp::Error &e) {
+    if (ctx) ctx->err = e.msg; else g_create_err = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    if (ctx) ctx->err = "host out of memory"; else g_create_err = "host out of memory";
+    return -2;
+  }
+}
+
+static void check_device_error(rp_ctx *c) {
+  int e = 0;
+  RP_CUDA(cudaMemcpyAsync(&e, c->errw.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  RP_CUDA(cudaStreamSynchronize(c->st));
+  if (e == 1) rp::fail(-3, "ntet.gt.nmax: a tetrahedron was cut into too many pieces");
+  if (e == 2) rp::fail(-3, "tetrahedron degeneracy classification failed (bad i3 / bad sum ia2)");
+  if (e == 3) rp::fail(-3, "dielectric matrix is singular");
+  if (e == 4) rp::fail(-3, "tensor-core contraction: wait limit reached");
+}
+
+static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const double *em, int nen_explicit) {
+  c->root = root ? root : ".";
+  c->S.params = *p;
+  RP_CUDA(cudaSetDevice(p->device));
+  c->dev = p->device;
+  RP_CUDA(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  for (auto &e : c->ev) RP_CUDA(cudaEventCreate(&e));
+  std::vector<double> emx;
+  for (int i = 0; i < 2 * nen_explicit; i++) emx.push_back(em[i]);
+  rp::read_dir_wfn(c->S, c->root);
+  rp::finish_setup(c->S, emx);
+  rp::read_wfn_coefficients(c->S, c->root);
+  if (p->flg_crpa == 1) rp::read_dir_wan_crpa(c->S, c->root);
+  rp::build_unfold_map(c->S, c->U);
+  rp::Setup &S = c->S;
+  for (int d = 0; d < 3; d++) c->R[d] = 0;
+  for (int j = 0; j < S.ntk; j++)
+    for (int ig = 0; ig < S.ng0[j]; ig++)
+      for (int d = 0; d < 3; d++) c->R[d] = std::max(c->R[d], std::abs(S.kg0[((size_t)j * S.ntg + ig) * 3 + d]));
+  cudaStream_t st = c->st;
+  upload(c->coef, S.coef, st);
+  upload(c->numirr, S.numirr, st);
+  upload(c->trs, S.trs, st);
+  upload(c->src, c->U.src, st);
+  upload(c->phase, c->U.phase, st);
+  upload(c->ng0, S.ng0, st);
+  upload(c->kg0, S.kg0, st);
+  upload(c->energy, S.e_eigi, st);
+  upload(c->prob, S.prob, st);
+  upload(c->imt1, S.imt1, st);
+  std::vector<int> idx2(S.index_kpt);
+  idx2.insert(idx2.end(), S.mesh_of_k.begin(), S.mesh_of_k.end());
+  upload(c->index2, idx2, st);
+  upload(c->em, S.em, st);
+  std::vector<double> b9(9);
+  for (int i = 0; i < 3; i++)
+    for (int d = 0; d < 3; d++) b9[3 * i + d] = S.b[i][d];
+  upload(c->b9, b9, st);
+  upload(c->sk0, S.sk0, st);
+  c->errw.ensure(16);
+  RP_CUDA(cudaMemsetAsync(c->errw.p, 0, 16, st));
+  const size_t N = (size_t)S.nw[0] * S.nw[1] * S.nw[2];
+  c->cfull.ensure(sizeof(cd) * (size_t)S.ntk * S.ncb * S.ntg);
+  c->ur.ensure(sizeof(float) * 2 * (size_t)S.ntk * S.ncb * N);
+  c->launches += rp::launch_wfn_realspace(c->coef.as<double2>(), c->numirr.as<int>(), c->trs.as<int>(),
+                                          c->src.as<int>(), c->phase.as<double2>(), c->ng0.as<int>(),
+                                          c->kg0.as<int>(), S.ntk, S.ncb, S.ntg, S.nw[0], S.nw[1], S.nw[2], c->R[0],
+                                          c->R[1], c->R[2], c->cfull.as<double2>(), c->ur.as<float2>(), 0, S.ntk, st);
+  RP_CUDA(cudaStreamSynchronize(st));
+}
+
+// Band pairs of one batch grouped by virtual band into chunks of <= jmax.
+static void build_chunks(const std::vector<int> &pvir, const std::vector<int> &pocc, int jmax,
+                         std::vector<int> &cv, std::vector<int> &cf, std::vector<int> &cc, std::vector<int> &plist) {
+  std::map<int, std::vector<int>> by;
+  for (size_t p = 0; p < pvir.size(); p++) by[pvir[p]].push_back((int)p);
+  cv.clear(); cf.clear(); cc.clear(); plist.clear();
+  for (auto &kv : by) {
+    const auto &v = kv.second;
+    for (size_t s = 0; s < v.size(); s += jmax) {
+      cv.push_back(kv.first);
+      cf.push_back((int)plist.size());
+      int n = (int)std::min<size_t>(jmax, v.size() - s);
+      cc.push_back(n);
+      for (int i = 0; i < n; i++) plist.push_back(v[s + i]);
+    }
+  }
+  (void)pocc;
+}
+
+static void chi0_q(rp_ctx *c, int iq, bool fast) {
+  rp::Setup &S = c->S;
+  cudaStream_t st = c->st;
+  c->have_chi = c->have_eps = false;
+  c->task = rp::make_qtask(S, iq - 1, S.params.max_pairs);
+  rp::QTask &t = c->task;
+  c->ndir = t.gamma ? 3 : 1;
+  const int ng = t.ng, nen = (int)S.em.size(), ntk = S.ntk;
+  upload(c->kpq, t.kpq, st);
+  upload(c->shift, t.shift, st);
+  upload(c->lg0, t.lg0, st);
+  upload(c->qglen, t.qglen, st);
+  RP_CUDA(cudaMemsetAsync(c->errw.p, 0, 16, st));
+  const size_t chisz = (size_t)c->ndir * nen * ng * ng;
+  c->chi.ensure(sizeof(cd) * chisz);
+  RP_CUDA(cudaMemsetAsync(c->chi.p, 0, sizeof(cd) * chisz, st));
+  if (t.gamma) {
+    c->rowcol.ensure(sizeof(cd) * 4 * (size_t)nen * ng);
+    RP_CUDA(cudaMemsetAsync(c->rowcol.p, 0, sizeof(cd) * 4 * (size_t)nen * ng, st));
+  }
+  int ep[3];
+  for (int d = 0; d < 3; d++) {
+    int r = 0;
+    for (int g = 0; g < ng; g++) r = std::max(r, std::abs(t.lg0[3 * g + d]));
+    ep[d] = r;
+  }
+  // pair batches sized so the per-batch buffers stay within a few GB
+  const int npair = (int)t.pair_vir.size();
+  const size_t per_pair = (size_t)ntk * (ng * sizeof(cd) + nen * sizeof(cd) + 3 * sizeof(cd));
+  const size_t budget = (size_t)6 << 30;
+  int bsz = (int)std::max<size_t>(1, std::min<size_t>(npair, budget / std::max<size_t>(per_pair, 1)));
+  // shared-memory limit of the pair-density tile decides how many pairs share one virtual band load
+  int jmax = 8;
+  const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];
+  auto smem_of = [&](int j, size_t elt) {
+    int D1 = 2 * ep[0] + 1 <= n1 ? 2 * ep[0] + 1 : n1, D2 = 2 * ep[1] + 1 <= n2 ? 2 * ep[1] + 1 : n2;
+    return elt * ((size_t)n1 + n2 + n3 + 2 * (size_t)n1 * n2 + (size_t)D1 * n2 + D1 * D2 + (size_t)j * ng) +
+           sizeof(int) * ((size_t)D1 + D2 + ng);
+  };
+  const size_t elt = fast ? sizeof(float) * 2 : sizeof(double) * 2;
+  while (jmax > 1 && smem_of(jmax, elt) > 220 * 1024) jmax--;
+  if (smem_of(jmax, elt) > 220 * 1024) rp::fail(1, "dielectric sphere (NG=%d) too large for the pair-density tile", ng);
+  float tms[4] = {0, 0, 0, 0};
+  RP_CUDA(cudaEventRecord(c->ev[5], st));
+  if (fast) rp::tc_begin_q(c->tcw, ng, nen, c->ndir, st);
+  for (int p0 = 0; p0 < npair; p0 += bsz) {
+    const int nb = std::min(bsz, npair - p0);
+    std::vector<int> bv(t.pair_vir.begin() + p0, t.pair_vir.begin() + p0 + nb);
+    std::vector<int> bo(t.pair_occ.begin() + p0, t.pair_occ.begin() + p0 + nb);
+    std::vector<int> cv, cf, cc, pl;
+    build_chunks(bv, bo, jmax, cv, cf, cc, pl);
+    upload(c->pvir, bv, st);
+    upload(c->pocc, bo, st);
+    upload(c->chunk_vir, cv, st);
+    upload(c->chunk_first, cf, st);
+    upload(c->chunk_count, cc, st);
+    upload(c->pair_list, pl, st);
+    // tetrahedron weights
+    rp::TetraArgs ta;
+    ta.ntk = ntk; ta.nen = nen; ta.ntb = S.ntb; ta.imt1 = c->imt1.as<int>(); ta.index_kpt = c->index2.as<int>();
+    ta.numirr = c->numirr.as<int>(); ta.kpq = c->kpq.as<int>(); ta.energy = c->energy.as<double>();
+    ta.prob = c->prob.as<double2>(); ta.em = c->em.as<double2>(); ta.pair_vir = c->pvir.as<int>();
+    ta.pair_occ = c->pocc.as<int>(); ta.npair = nb; ta.efermi = S.efermi; ta.delt = S.delt; ta.dmna = S.dmna;
+    ta.dmnr = S.dmnr; ta.err = c->errw.as<int>();
+    c->wts.ensure(sizeof(cd) * (size_t)nb * nen * ntk);
+    RP_CUDA(cudaEventRecord(c->ev[0], st));
+    c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st);
+    RP_CUDA(cudaEventRecord(c->ev[1], st));
+    rp::PairGeom pg;
+    pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;
+    pg.kpq = c->kpq.as<int>(); pg.shift = c->shift.as<int>(); pg.lg0 = c->lg0.as<int>();
+    pg.R1 = ep[0]; pg.R2 = ep[1]; pg.R3 = ep[2];
+    rp::PairChunks pc;
+    pc.chunk_vir = c->chunk_vir.as<int>(); pc.chunk_first = c->chunk_first.as<int>();
+    pc.chunk_count = c->chunk_count.as<int>(); pc.pair_list = c->pair_list.as<int>();
+    pc.pair_occ = c->pocc.as<int>(); pc.nchunk = (int)cv.size(); pc.jmax = jmax;
+    if (t.gamma) {
+      c->head.ensure(sizeof(cd) * 3 * (size_t)nb * ntk);
+      c->launches += rp::launch_gamma_head(c->cfull.as<double2>(), c->ng0.as<int>(), c->kg0.as<int>(), ntk, S.ncb,
+                                           S.ntg, c->b9.as<double>(), c->energy.as<double>(), S.ntb,
+                                           c->numirr.as<int>(), c->pvir.as<int>(), c->pocc.as<int>(), nb, S.delt,
+                                           c->head.as<double2>(), st);
+    }
+    if (!fast) {
+      c->rho.ensure(sizeof(cd) * (size_t)nb * ntk * ng);
+      c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
+      RP_CUDA(cudaEventRecord(c->ev[2], st));
+      if (t.gamma) {
+        c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
+                                               ntk, ng, nen, t.no_g0, c->rowcol.as<double2>(), st);
+        c->launches += rp::launch_set_head(c->rho.as<double2>(), c->head.as<double2>(), nb, ntk, ng, t.no_g0, 0, st);
+      }
+      c->launches += rp::launch_contract_fp64(c->rho.as<double2>(), c->wts.as<double2>(), nb, ntk, ng, nen,
+                                              c->chi.as<double2>(), st);
+    } else {
+      c->rho.ensure(sizeof(float) * 2 * (size_t)nb * ntk * ng);
+      c->launches += rp::launch_pair_density_fp32(c->ur.as<float2>(), pg, pc, c->rho.as<float2>(), st);
+      RP_CUDA(cudaEventRecord(c->ev[2], st));
+      c->launches += rp::tc_contract_batch(c->tcw, c->rho.as<float2>(), c->wts.as<double2>(),
+                                           t.gamma ? c->head.as<double2>() : nullptr, nb, ntk, ng, nen, t.no_g0,
+                                           S.params.precision, c->chi.as<double2>(),
+                                           t.gamma ? c->rowcol.as<double2>() : nullptr, c->errw.as<int>(), st);
+    }
+    RP_CUDA(cudaEventRecord(c->ev[3], st));
+    RP_CUDA(cudaEventSynchronize(c->ev[3]));
+    float a = 0, b = 0, d = 0;
+    RP_CUDA(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+    RP_CUDA(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+    RP_CUDA(cudaEventElapsedTime(&d, c->ev[2], c->ev[3]));
+    tms[0] += a; tms[1] += b; tms[2] += d;
+  }
+  if (fast) c->launches += rp::tc_end_q(c->tcw, c->chi.as<double2>(), t.gamma ? c->rowcol.as<double2>() : nullptr, st);
+  // Gamma: directions 2 and 3 share the body of direction 1 and get their own G=0 row/column
+  if (t.gamma) {
+    const size_t m = (size_t)nen * ng * ng;
+    double2 *chi = c->chi.as<double2>();
+    RP_CUDA(cudaMemcpyAsync(chi + m, chi, sizeof(cd) * m, cudaMemcpyDeviceToDevice, st));
+    RP_CUDA(cudaMemcpyAsync(chi + 2 * m, chi, sizeof(cd) * m, cudaMemcpyDeviceToDevice, st));
+    std::vector<cd> rc(4 * (size_t)nen * ng);
+    RP_CUDA(cudaMemcpyAsync(rc.data(), c->rowcol.p, sizeof(cd) * rc.size(), cudaMemcpyDeviceToHost, st));
+    RP_CUDA(cudaStreamSynchronize(st));
+    for (int ix = 1; ix <= 2; ix++)
+      for (int e = 0; e < nen; e++) {
+        const cd *row = &rc[(((size_t)(ix - 1) * nen + e) * 2) * ng], *col = row + ng;
+        double2 *base = chi + (size_t)ix * m + (size_t)e * ng * ng;
+        // row G0: element (G0, g') at G0 + ng*g'; column G0: element (g, G0) at g + ng*G0
+        std::vector<double2> rr(ng), cl(ng);
+        for (int g = 0; g < ng; g++) { rr[g] = make_double2(row[g].real(), row[g].imag()); cl[g] = make_double2(col[g].real(), col[g].imag()); }
+        RP_CUDA(cudaMemcpy2DAsync(base + t.no_g0, sizeof(double2) * ng, rr.data(), sizeof(double2), sizeof(double2), ng,
+                                  cudaMemcpyHostToDevice, st));
+        RP_CUDA(cudaMemcpyAsync(base + (size_t)ng * t.no_g0, cl.data(), sizeof(double2) * ng, cudaMemcpyHostToDevice, st));
+        RP_CUDA(cudaStreamSynchronize(st));
+      }
+  }
+  c->launches += rp::launch_scale(c->chi.as<double2>(), chisz, S.volume, st);
+  // Drude plasma frequency from the intraband pairs (metals, fRPA only)
+  c->wd[0] = c->wd[1] = c->wd[2] = 0;
+  if (t.gamma && !t.intra_band.empty()) {
+    upload(c->intra, t.intra_band, st);
+    c->pwpl.ensure(sizeof(cd) * 3);
+    RP_CUDA(cudaMemsetAsync(c->pwpl.p, 0, sizeof(cd) * 3, st));
+    rp::TetraArgs ta;
+    ta.ntk = ntk; ta.nen = nen; ta.ntb = S.ntb; ta.imt1 = c->imt1.as<int>(); ta.index_kpt = c->index2.as<int>();
+    ta.numirr = c->numirr.as<int>(); ta.kpq = c->kpq.as<int>(); ta.energy = c->energy.as<double>();
+    ta.prob = c->prob.as<double2>(); ta.em = c->em.as<double2>(); ta.pair_vir = nullptr; ta.pair_occ = nullptr;
+    ta.npair = 0; ta.efermi = S.efermi; ta.delt = S.delt; ta.dmna = S.dmna; ta.dmnr = S.dmnr;
+    ta.err = c->errw.as<int>();
+    c->launches += rp::launch_intraband(ta, c->cfull.as<double2>(), c->ng0.as<int>(), c->kg0.as<int>(), S.ncb,
+                                        S.ntg, c->b9.as<double>(), c->sk0.as<double>(), c->intra.as<int>(),
+                                        (int)t.intra_band.size(), c->pwpl.as<double2>(), st);
+    cd pw[3];
+    RP_CUDA(cudaMemcpyAsync(pw, c->pwpl.p, sizeof(cd) * 3, cudaMemcpyDeviceToHost, st));
+    RP_CUDA(cudaStreamSynchronize(st));
+    for (int d = 0; d < 3; d++) {
+      cd wpl = 8.0 * pw[d] / S.volume / (double)ntk;
+      c->wd[d] = std::sqrt(wpl.real());
+    }
+  }
+  RP_CUDA(cudaEventRecord(c->ev[4], st));
+  check_device_error(c);
+  float tot = 0;
+  RP_CUDA(cudaEventElapsedTime(&tot, c->ev[5], c->ev[4]));
+  c->times[0] = tms[0] * 1e-3; c->times[1] = tms[1] * 1e-3; c->times[2] = tms[2] * 1e-3; c->times[4] = tot * 1e-3;
+  c->have_chi = true;
+}
+
+static void epsinv_run(rp_ctx *c) {
+  if (!c->have_chi) rp::fail(1, "rp_epsinv_q needs a preceding rp_chi0_q");
+  rp::QTask &t = c->task;
+  const int ng = t.ng, nen = (int)c->S.em.size(), nmat = c->ndir * nen;
+  const size_t sz = (size_t)nmat * ng * ng;
+  cudaStream_t st = c->st;
+  c->A.ensure(sizeof(cd) * sz);
+  c->eps.ensure(sizeof(cd) * sz);
+  c->prow.ensure(sizeof(cd) * (size_t)nmat * ng);
+  c->fcol.ensure(sizeof(cd) * (size_t)nmat * ng);
+  c->piv.ensure(sizeof(int) * (size_t)nmat * ng);
+  c->used.ensure(sizeof(int) * (size_t)nmat * ng);
+  rp::EpsArgs a;
+  a.ng = ng; a.nen = nen; a.ndir = c->ndir; a.gamma = t.gamma; a.g0 = t.no_g0; a.qglen = c->qglen.as<double>();
+  a.em = c->em.as<double2>(); a.delt = c->S.delt;
+  for (int d = 0; d < 3; d++) a.wd[d] = c->wd[d];
+  RP_CUDA(cudaEventRecord(c->ev[0], st));
+  c->launches += rp::launch_eps_build(c->chi.as<double2>(), a, c->A.as<double2>(), st);
+  c->launches += rp::launch_gauss_jordan(c->A.as<double2>(), ng, nmat, c->prow.as<double2>(), c->fcol.as<double2>(),
+                                         c->piv.as<int>(), c->used.as<int>(), c->eps.as<double2>(), c->errw.as<int>(), st);
+  RP_CUDA(cudaEventRecord(c->ev[1], st));
+  check_device_error(c);
+  float ms = 0;
+  RP_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->times[3] = ms * 1e-3;
+  c->have_eps = true;
+}
+
+static void fetch(rp_ctx *c, DevBuf &b, std::vector<cd> &h) {
+  const rp::QTask &t = c->task;
+  h.resize((size_t)c->ndir * c->S.em.size() * t.ng * t.ng);
+  RP_CUDA(cudaMemcpyAsync(h.data(), b.p, sizeof(cd) * h.size(), cudaMemcpyDeviceToHost, c->st));
+  RP_CUDA(cudaStreamSynchronize(c->st));
+}
+
+static void mkdir_p(const std::string &p) { mkdir(p.c_str(), 0755); }
+
+static void write_q(rp_ctx *c, const std::string &root) {
+  if (!c->have_eps) rp::fail(1, "rp_write_q needs rp_chi0_q and rp_epsinv_q first");
+  rp::Setup &S = c->S;
+  rp::QTask &t = c->task;
+  const int ng = t.ng, nen = (int)S.em.size();
+  fetch(c, c->eps, c->h_eps);
+  int qnum = -1;
+  for (int ik = 0; ik < S.nk_irr; ik++)
+    if (std::fabs(S.ski_list[3 * ik] - t.q[0]) < 1e-6 && std::fabs(S.ski_list[3 * ik + 1] - t.q[1]) < 1e-6 &&
+        std::fabs(S.ski_list[3 * ik + 2] - t.q[2]) < 1e-6)
+      qnum = ik + 1;
+  char buf[64];
+  snprintf(buf, sizeof buf, "q%03d", qnum);
+  const std::string epsdir = root + "/dir-eps", qdir = epsdir + "/" + buf;
+  mkdir_p(epsdir);
+  mkdir_p(qdir);
+  if (S.params.dump_chi) {
+    fetch(c, c->chi, c->h_chi);
+    FILE *f = fopen((qdir + "/dat.chi0").c_str(), "wb");
+    if (!f) rp::fail(1, "cannot write %s/dat.chi0", qdir.c_str());
+    int32_t hdr[4] = {ng, nen, c->ndir, (int32_t)t.pair_vir.size()};
+    fwrite(hdr, 4, 4, f);
+    fwrite(c->h_chi.data(), sizeof(cd), c->h_chi.size(), f);
+    fclose(f);
+  }
+  {
+    FILE *f = fopen((qdir + "/dat.sq").c_str(), "w");
+    if (!f) rp::fail(1, "cannot write %s/dat.sq", qdir.c_str());
+    fprintf(f, " %24.16E %24.16E %24.16E\n", t.q[0], t.q[1], t.q[2]);
+    fclose(f);
+  }
+  const size_t m = (size_t)nen * ng * ng;
+  for (int ix = 0; ix < c->ndir; ix++) {
+    const int base = S.params.file_num_eps_base_start + ix * 1000;
+    for (int e = 0; e < nen; e++) {
+      snprintf(buf, sizeof buf, "/dat.epsqw.%06d", base + e + 1);
+      FILE *f = fopen((qdir + buf).c_str(), "w");
+      if (!f) rp::fail(1, "cannot write %s%s", qdir.c_str(), buf);
+      fprintf(f, "#epsqw diagonal term\n#1:q+G [au], 2:Re(eps-1), 3:Im(eps-1)\n");
+      const cd *E = &c->h_eps[ix * m + (size_t)e * ng * ng];
+      for (int g = 0; g < ng; g++)
+        fprintf(f, "%20.10f%20.10f%20.10f\n", t.qglen[g], E[g + (size_t)ng * g].real(), E[g + (size_t)ng * g].imag());
+      fclose(f);
+    }
+    snprintf(buf, sizeof buf, "/dat.epsqw.%03d", S.params.file_num_eps_start + ix);
+    rp::write_unformatted_record(qdir + buf, &c->h_eps[ix * m], sizeof(cd) * m);
+  }
+  // the completion flag is written last, so an interrupted run resumes at this q
+  snprintf(buf, sizeof buf, "/dat.log.%03d", S.params.file_num_log_start);
+  FILE *f = fopen((qdir + buf).c_str(), "w");
+  if (!f) rp::fail(1, "cannot write %s%s", qdir.c_str(), buf);
+  fprintf(f, " #\n #finish chi0 evaluation for %11d\n #\n", qnum);
+  fclose(f);
+}
+
+extern "C" {
+
+int rp_ctx_create(rp_ctx **out, const char *root, const rp_params *p, const double *em, int nen_explicit) {
+  if (!out || !p) return 1;
+  *out = nullptr;
+  std::unique_ptr<rp_ctx> c(new rp_ctx());
+  int rc = guarded(nullptr, [&] { create_ctx(c.get(), root, p, em, nen_explicit); });
+  if (rc) return rc;
+  *out = c.release();
+  return 0;
+}
+
+int rp_ctx_info(const rp_ctx *c, rp_info *info) {
+  if (!c || !info) return 1;
+  const rp::Setup &S = c->S;
+  info->ntk = S.ntk; info->nk_irr = S.nk_irr; info->ntg = S.ntg; info->ntb = S.ntb; info->ncb = S.ncb;
+  for (int d = 0; d < 3; d++) { info->nkb[d] = S.nkb[d]; info->fft_box[d] = S.nw[d]; }
+  info->nen = (int)S.em.size();
+  info->n_occ = S.n_occ; info->n_vir = S.n_vir; info->n_docc = S.n_docc; info->n_pocc = S.n_pocc; info->n_uocc = S.n_uocc;
+  info->volume = S.volume; info->efermi = S.efermi; info->ecut_psi = S.ecut_psi; info->ecut_eps = S.ecut_eps;
+  double bytes = 0;
+  for (const DevBuf *b : {&c->coef, &c->cfull, &c->ur, &c->wts, &c->rho, &c->chi, &c->A, &c->eps, &c->src, &c->phase,
+                          &c->kg0})
+    bytes += (double)b->bytes;
+  info->device_bytes = bytes + (double)c->tcw.bytes();
+  return 0;
+}
+
+int rp_num_qirr(const rp_ctx *c) { return c ? c->S.nk_irr : 0; }
+
+int rp_chi0_q(rp_ctx *c, int iq, double *chi, int *ng_out, int *ndir_out) {
+  if (!c) return 1;
+  return guarded(c, [&] {
+    RP_CUDA(cudaSetDevice(c->dev));
+    chi0_q(c, iq, c->S.params.precision != RP_PREC_FP64);
+    if (ng_out) *ng_out = c->task.ng;
+    if (ndir_out) *ndir_out = c->ndir;
+    if (chi) {
+      fetch(c, c->chi, c->h_chi);
+      std::memcpy(chi, c->h_chi.data(), sizeof(cd) * c->h_chi.size());
+    }
+  });
+}
+
+int rp_epsinv_q(rp_ctx *c, double *epsinv) {
+  if (!c) return 1;
+  return guarded(c, [&] {
+    RP_CUDA(cudaSetDevice(c->dev));
+    epsinv_run(c);
+    if (epsinv) {
+      fetch(c, c->eps, c->h_eps);
+      std::memcpy(epsinv, c->h_eps.data(), sizeof(cd) * c->h_eps.size());
+    }
+  });
+}
+
+int rp_write_q(rp_ctx *c, const char *root) {
+  if (!c) return 1;
+  return guarded(c, [&] { write_q(c, root ? root : c->root); });
+}
+
+int rp_stage_times(const rp_ctx *c, double *t5) {
+  if (!c || !t5) return 1;
+  for (int i = 0; i < 5; i++) t5[i] = c->times[i];
+  return 0;
+}
+
+long long rp_kernel_launches(const rp_ctx *c) { return c ? c->launches : 0; }
+
+const char *rp_last_error(const rp_ctx *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
+
+void rp_ctx_destroy(rp_ctx *c) { delete c; }
+
+int rp_calc_chiqw(const char *root, const char *namelist_text) {
+  rp_params p;
+  rp_default_params(&p);
+  std::vector<int> qlist;
+  std::vector<double> em;
+  int rc = guarded(nullptr, [&] { rp::parse_namelist_text(namelist_text ? namelist_text : "", &p, &qlist, &em); });
+  if (rc) return rc;
+  rp_ctx *c = nullptr;
+  rc = rp_ctx_create(&c, root, &p, em.data(), (int)em.size() / 2);
+  if (rc) return rc;
+  rc = guarded(c, [&] {
+    rp::Setup &S = c->S;
+    const std::string epsdir = std::string(root) + "/dir-eps";
+    mkdir_p(epsdir);
+    char buf[64];
+    for (int ik = 0; ik < S.nk_irr; ik++) { snprintf(buf, sizeof buf, "/q%03d", ik + 1); mkdir_p(epsdir + buf); }
+    std::vector<int> todo;
+    if (p.flg_calc_type == 2) {
+      struct stat stt;
+      for (int ik : qlist) {
+        if (ik < 1 || ik > S.nk_irr) rp::fail(1, "q index %d outside dat.sample-k", ik);
+        snprintf(buf, sizeof buf, "/q%03d/dat.log.%03d", ik, p.file_num_log_start);
+        if (stat((epsdir + buf).c_str(), &stt) != 0) todo.push_back(ik - 1);
+      }
+    } else {
+      todo = rp::q_list(S, epsdir);
+    }
+    // shared files (chiqw.F:1206-1215)
+    FILE *f = fopen((epsdir + "/dat.chi_cutoff").c_str(), "w");
+    if (f) { fprintf(f, " %24.16E\n", S.ecut_eps); fclose(f); }
+    f = fopen((epsdir + "/dat.wgrid").c_str(), "w");
+    if (f) {
+      fprintf(f, " %11d\n", (int)S.em.size());
+      for (auto &e : S.em) fprintf(f, "%15.10f%15.10f\n", e.real(), e.imag());
+      fclose(f);
+    }
+    const int ns = std::max(1, p.qshard_count), si = p.qshard_index;
+    for (size_t i = 0; i < todo.size(); i++) {
+      if ((int)(i % ns) != si) continue;
+      chi0_q(c, todo[i] + 1, p.precision != RP_PREC_FP64);
+      epsinv_run(c);
+      write_q(c, root);
+    }
+  });
+  if (rc) g_create_err = c->err;
+  rp_ctx_destroy(c);
+  return rc;
+}
+
+}  // extern "C"

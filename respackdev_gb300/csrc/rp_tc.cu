@@ -1,0 +1,534 @@
+// rp_tc.cu -- chi0 contraction on the 5th-generation tensor cores (tcgen05).
+//
+// Per frequency w the contraction of chiqw.F:1397-1410 is
+//     chi_w = rho^H diag(x_w) rho,   x_w(K) = xow(k,w) (1 - P P)/NTK,  K = (pair, k).
+// With Y the real matrix whose rows are Re rho(G) (rows 0..Gp) and Im rho(G)
+// (rows Gp..2Gp), and M_x = Y diag(x) Y^T,
+//     Re chi = Mr.rr + Mr.ii - Mi.ri + Mi.ir,   Im chi = Mi.rr + Mi.ii + Mr.ri - Mr.ir
+// (Mr, Mi: x = Re / Im of the weight; rr, ri, ir, ii: quadrants of M).  M is
+// symmetric, so only tiles on or above the diagonal are computed.
+//
+// Precision: each operand value v is split into two FP16 terms v = hi + lo
+// (RP_PREC_FP16X2: products hi.hi + hi.lo + lo.hi) or three BF16 terms
+// (RP_PREC_BF16X3: the six products with i + j <= 2), after scaling the batch
+// by powers of two so FP16 stays in range.  The tensor cores accumulate in
+// FP32 in tensor memory over a sub-chunk of K; the epilogue warps then add the
+// sub-chunk into an FP64 copy of the tile in global memory, so FP32 rounding
+// never sees more than one sub-chunk.
+//
+// Kernel layout (one CTA per (frequency, upper tile)), 288 threads:
+//   warps 0-3  producers: read FP32 rho and the weights, scale, split and store
+//              the operand tiles into shared memory in the 128-byte-swizzled
+//              K-major layout the tensor core reads;
+//   warps 4-7  epilogue: drain the FP32 accumulators from tensor memory
+//              (tcgen05.ld) into the FP64 tile;
+//   warp 8     allocates tensor memory and issues tcgen05.mma (one thread).
+// Two operand stages and two accumulator buffers (2 channels x 128 columns
+// each, all 512 TMEM columns) overlap production, MMA and draining.  Every
+// mbarrier wait is bounded; on timeout the CTA raises the error word, waits
+// (bounded) for its own MMAs and frees tensor memory before returning.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "rp_dev.cuh"
+#include "rp_host.h"
+#include "rp_tc.h"
+
+namespace rp {
+
+namespace {
+
+constexpr int BM = 128;          // tile rows (a) = TMEM lanes
+constexpr int BN = 128;          // tile columns (b)
+constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
+constexpr int NSTAGE = 2;
+constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
+constexpr int NPROD = 128, NEPI = 128;
+constexpr int NTHREADS = NPROD + NEPI + 32;
+constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
+
+struct TcArgs {
+  const float *Yt;        // [Mp][Kp] rows: Re rho (0..Gp), Im rho (Gp..2Gp)
+  const float2 *wt;       // [nen][Kp] weights
+  const float *maxes;     // [0] = max|Y|, [1 + 2e] = max|Re w_e|, [2 + 2e] = max|Im w_e|
+  double *M64;            // [nen][2][Mp][Mp] FP64 tiles (upper triangle used)
+  int *err;
+  int Mp, Kp, nen, ntile_side, ksub_blocks, nplanes, bf16;
+  const int2 *tiles;      // (ta, tb) list, ta <= tb
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *b, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait; returns false (and raises the abort flag) when it gives up
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag) {
+  for (long i = 0; i < WAIT_LIMIT; i++) {
+    if (mbar_try(b, parity)) return true;
+    if (*abort_flag) return false;
+    if (i > 64) __nanosleep(32);
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms of 1024 bytes
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);       // start address
+  d |= (uint64_t)1 << 16;                         // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                         // descriptor version
+  d |= (uint64_t)2 << 61;                         // SWIZZLE_128B
+  return d;
+}
+// instruction descriptor of kind::f16: D f32, A/B f16 (0) or bf16 (1), both K-major
+__host__ __device__ constexpr uint32_t make_idesc(int bf16, int M, int N) {
+  return (1u << 4) | ((uint32_t)bf16 << 7) | ((uint32_t)bf16 << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+}
+__device__ __forceinline__ void mma_commit(uint64_t *b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// power-of-two scale that maps |v| <= vmax to <= 2^14
+__device__ __forceinline__ float scale_for(float vmax) {
+  if (!(vmax > 0.f)) return 1.f;
+  int e;
+  frexpf(vmax, &e);  // vmax = m 2^e, m in [0.5, 1)
+  return ldexpf(1.f, 14 - e);
+}
+
+// split v into nplanes 16-bit terms (fp16 x2 or bf16 x3), returned as raw bits
+__device__ __forceinline__ void split16(float v, int nplanes, int bf16, uint16_t *t) {
+  float r = v;
+  for (int p = 0; p < nplanes; p++) {
+    if (bf16) {
+      __nv_bfloat16 h = __float2bfloat16_rn(r);
+      t[p] = __bfloat16_as_ushort(h);
+      r = r - __bfloat162float(h);
+    } else {
+      __half h = __float2half_rn(r);
+      t[p] = __half_as_ushort(h);
+      r = r - __half2float(h);
+    }
+  }
+}
+
+// byte offset of element (row, k) of a 128 x 64 16-bit tile in the 128B-swizzled K-major layout
+__device__ __forceinline__ uint32_t swz(int row, int chunk16) {
+  return (uint32_t)(row * 128 + ((chunk16 ^ (row & 7)) << 4));
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-align the operand area
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int np = a.nplanes;                       // 2 (fp16) or 3 (bf16)
+  const int tiles_per_stage = np + 2 * np;        // B planes + 2 channels x A planes
+  unsigned char *stage_base = smem;
+  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES);
+  uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accempty = bars + 6, *fin = bars + 8;
+  volatile int *abort_flag = (volatile int *)(bars + 9);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 10);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int e = blockIdx.y;
+  const int2 tt = a.tiles[blockIdx.x];
+  const int ta = tt.x, tb = tt.y;
+  const int nkb = a.Kp / BK;
+  const int nsub = (nkb + a.ksub_blocks - 1) / a.ksub_blocks;
+
+  if (tid == 0) {
+    mbar_init(&full[0], NPROD); mbar_init(&full[1], NPROD);
+    mbar_init(&empty[0], 1); mbar_init(&empty[1], 1);
+    mbar_init(&accfull[0], 1); mbar_init(&accfull[1], 1);
+    mbar_init(&accempty[0], NEPI); mbar_init(&accempty[1], NEPI);
+    mbar_init(fin, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const float ymax = a.maxes[0];
+  const float sB = scale_for(ymax);
+  const float sA0 = scale_for(ymax * a.maxes[1 + 2 * e]);
+  const float sA1 = scale_for(ymax * a.maxes[2 + 2 * e]);
+
+  if (warp < 4) {
+    // ---------------- producers: one operand row per thread ----------------
+    const int r = tid;  // 0..127
+    const float *ya = a.Yt + (size_t)(ta * BM + r) * a.Kp;
+    const float *yb = a.Yt + (size_t)(tb * BM + r) * a.Kp;
+    const float2 *wt = a.wt + (size_t)e * a.Kp;
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb & 1, use = kb >> 1;
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
+      unsigned char *st = stage_base + (size_t)s * tiles_per_stage * TILE_BYTES;
+      const int k0 = kb * BK;
+#pragma unroll 1
+      for (int c = 0; c < 8; c++) {  // 8 chunks of 8 K values
+        const float4 *pa = (const float4 *)(ya + k0 + 8 * c), *pb = (const float4 *)(yb + k0 + 8 * c);
+        float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), b0 = __ldg(pb), b1 = __ldg(pb + 1);
+        float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        uint16_t tb16[3][8], t0[3][8], t1[3][8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const float2 w = __ldg(wt + k0 + 8 * c + j);
+          uint16_t t[3];
+          split16(bv[j] * sB, np, a.bf16, t);
+          for (int p = 0; p < np; p++) tb16[p][j] = t[p];
+          split16(av[j] * w.x * sA0, np, a.bf16, t);
+          for (int p = 0; p < np; p++) t0[p][j] = t[p];
+          split16(av[j] * w.y * sA1, np, a.bf16, t);
+          for (int p = 0; p < np; p++) t1[p][j] = t[p];
+        }
+        const uint32_t off = swz(r, c);
+        for (int p = 0; p < np; p++) {
+          uint4 vb, v0, v1;
+          vb.x = tb16[p][0] | ((uint32_t)tb16[p][1] << 16); vb.y = tb16[p][2] | ((uint32_t)tb16[p][3] << 16);
+          vb.z = tb16[p][4] | ((uint32_t)tb16[p][5] << 16); vb.w = tb16[p][6] | ((uint32_t)tb16[p][7] << 16);
+          v0.x = t0[p][0] | ((uint32_t)t0[p][1] << 16); v0.y = t0[p][2] | ((uint32_t)t0[p][3] << 16);
+          v0.z = t0[p][4] | ((uint32_t)t0[p][5] << 16); v0.w = t0[p][6] | ((uint32_t)t0[p][7] << 16);
+          v1.x = t1[p][0] | ((uint32_t)t1[p][1] << 16); v1.y = t1[p][2] | ((uint32_t)t1[p][3] << 16);
+          v1.z = t1[p][4] | ((uint32_t)t1[p][5] << 16); v1.w = t1[p][6] | ((uint32_t)t1[p][7] << 16);
+          // tile order in a stage: B planes, then channel 0 A planes, then channel 1 A planes
+          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = vb;
+          *(uint4 *)(st + (size_t)(np + p) * TILE_BYTES + off) = v0;
+          *(uint4 *)(st + (size_t)(2 * np + p) * TILE_BYTES + off) = v1;
+        }
+      }
+      fence_proxy_async();
+      mbar_arrive(&full[s]);
+    }
+  } else if (warp < 8) {
+    // ---------------- epilogue: drain FP32 sub-chunk sums into FP64 ----------------
+    const int q = warp - 4;                 // TMEM lanes 32q..32q+31
+    const int row = ta * BM + 32 * q + lane;
+    for (int sc = 0; sc < nsub; sc++) {
+      const int b = sc & 1, use = sc >> 1;
+      if (!mbar_wait(&accfull[b], use & 1, abort_flag)) break;
+      tc_fence_after();
+      for (int ch = 0; ch < 2; ch++) {
+        const double inv = 1.0 / ((double)sB * (double)(ch == 0 ? sA0 : sA1));
+        double *dst = a.M64 + (((size_t)e * 2 + ch) * a.Mp + row) * a.Mp + tb * BN;
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          float v[32];
+          tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((b * 2 + ch) * BN + c0), v);
+#pragma unroll 4
+          for (int j = 0; j < 32; j++) dst[c0 + j] += (double)v[j] * inv;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&accempty[b]);
+    }
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    const uint32_t idesc = make_idesc(a.bf16, BM, BN);
+    int kb = 0;
+    for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
+      const int b = sc & 1, buse = sc >> 1;
+      if (buse > 0 && !mbar_wait(&accempty[b], (buse - 1) & 1, abort_flag)) break;
+      tc_fence_after();
+      const int kend = min(nkb, (sc + 1) * a.ksub_blocks);
+      bool first = true;
+      for (; kb < kend; kb++) {
+        const int s = kb & 1, use = kb >> 1;
+        if (!mbar_wait(&full[s], use & 1, abort_flag)) break;
+        tc_fence_after();
+        const uint32_t st = smem_u32(stage_base + (size_t)s * tiles_per_stage * TILE_BYTES);
+        for (int kk = 0; kk < BK / 16; kk++) {
+          for (int ch = 0; ch < 2; ch++) {
+            const uint32_t d = tmem + (uint32_t)((b * 2 + ch) * BN);
+            // products with plane(A) + plane(B) <= np - 1
+            for (int pa = 0; pa < np; pa++)
+              for (int pb = 0; pa + pb < np; pb++) {
+                const uint64_t ad = make_desc(st + (uint32_t)((np * (1 + ch) + pa) * TILE_BYTES) + kk * 32);
+                const uint64_t bd = make_desc(st + (uint32_t)(pb * TILE_BYTES) + kk * 32);
+                mma_f16(d, ad, bd, idesc, first ? 0 : 1);
+                first = false;
+              }
+            if (ch == 0) first = (kb == sc * a.ksub_blocks && kk == 0);  // channel 1 starts fresh too
+          }
+          first = false;
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(&accfull[b]);
+    }
+    // wait for every MMA this thread issued before tensor memory is released
+    mma_commit(fin);
+    mbar_wait(fin, 0, abort_flag);
+  }
+  if (tid == 0 && *abort_flag) atomicExch(a.err, 4);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// helpers: transpose the batch's pair densities and weights into the GEMM's
+// K-major operands, batch maxima, Gamma rows/columns, final assembly.
+
+// Yt[g][K] = Re rho, Yt[Gp+g][K] = Im rho, K = k*npair + p (rho is [p][k][g])
+__global__ void yt_kernel(const float2 *__restrict__ rho, int npair, int ntk, int ng, int Gp, int Kp,
+                          float *__restrict__ Yt, const double2 *__restrict__ head, int g0) {
+  const long K = (long)blockIdx.x;  // one K per block
+  const int k = (int)(K / npair), p = (int)(K % npair);
+  const float2 *src = rho + ((size_t)p * ntk + k) * ng;
+  for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+    float2 v = src[g];
+    if (head && g == g0) {
+      double2 h = head[((size_t)p * ntk + k) * 3];
+      v = make_float2((float)h.x, (float)h.y);
+    }
+    Yt[(size_t)g * Kp + K] = v.x;
+    Yt[(size_t)(Gp + g) * Kp + K] = v.y;
+  }
+}
+
+// wt[e][K] = w[(p*nen + e)*ntk + k]
+__global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int nen, int Kp, float2 *__restrict__ wt) {
+  const long K = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (K >= (long)npair * ntk) return;
+  const int k = (int)(K / npair), p = (int)(K % npair);
+  for (int e = 0; e < nen; e++) {
+    double2 v = w[((size_t)p * nen + e) * ntk + k];
+    wt[(size_t)e * Kp + K] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
+  atomicMax((int *)addr, __float_as_int(v));  // valid for non-negative floats
+}
+
+__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float2 *__restrict__ wt, int nen, int Kp,
+                             long Kn, float *__restrict__ out) {
+  float m = 0.f;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nY; i += (size_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(Yt[i]));
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_pos(&out[0], m);
+  for (int e = 0; e < nen; e++) {
+    float mr = 0.f, mi = 0.f;
+    for (long K = (long)blockIdx.x * blockDim.x + threadIdx.x; K < Kn; K += (long)gridDim.x * blockDim.x) {
+      float2 v = wt[(size_t)e * Kp + K];
+      mr = fmaxf(mr, fabsf(v.x));
+      mi = fmaxf(mi, fabsf(v.y));
+    }
+    for (int o = 16; o; o >>= 1) {
+      mr = fmaxf(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+      mi = fmaxf(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    }
+    if ((threadIdx.x & 31) == 0) { atomic_max_pos(&out[1 + 2 * e], mr); atomic_max_pos(&out[2 + 2 * e], mi); }
+  }
+}
+
+// Gamma, directions 2 and 3: G=0 row and column in FP64 from the FP32 densities
+__global__ void gamma_rowcol_f32_kernel(const float2 *__restrict__ rho, const double2 *__restrict__ w,
+                                        const double2 *__restrict__ head, int npair, int ntk, int ng, int nen, int g0,
+                                        double2 *__restrict__ rowcol) {
+  const int g = blockIdx.x, e = blockIdx.y, ix = blockIdx.z + 1;
+  const long K = (long)npair * ntk;
+  double2 r = make_double2(0, 0), c = make_double2(0, 0);
+  for (long Kx = threadIdx.x; Kx < K; Kx += blockDim.x) {
+    const int p = (int)(Kx / ntk), k = (int)(Kx % ntk);
+    const double2 ww = w[((size_t)p * nen + e) * ntk + k];
+    const double2 h = head[(size_t)Kx * 3 + ix];
+    double2 v;
+    if (g == g0) v = h;
+    else { float2 f = rho[(size_t)Kx * ng + g]; v = make_double2(f.x, f.y); }
+    cfma(r, cmul(ww, cconj(h)), v);
+    cfma(c, cmul(ww, cconj(v)), h);
+  }
+  __shared__ double2 sr[256], sc[256];
+  sr[threadIdx.x] = r;
+  sc[threadIdx.x] = c;
+  __syncthreads();
+  for (int s = 128; s; s >>= 1) {
+    if (threadIdx.x < s) {
+      sr[threadIdx.x] = cadd(sr[threadIdx.x], sr[threadIdx.x + s]);
+      sc[threadIdx.x] = cadd(sc[threadIdx.x], sc[threadIdx.x + s]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double2 *o = rowcol + ((size_t)(ix - 1) * nen + e) * 2 * ng;
+    o[g] = cadd(o[g], sr[0]);
+    o[ng + g] = cadd(o[ng + g], sc[0]);
+  }
+}
+
+__device__ __forceinline__ double mget(const double *M, int Mp, int i, int j) {
+  // symmetric matrix stored in its upper tiles
+  const int ti = i / BM, tj = j / BN;
+  return ti <= tj ? M[(size_t)i * Mp + j] : M[(size_t)j * Mp + i];
+}
+
+// chi[e][g + ng h] = (Mr.rr + Mr.ii - Mi.ri + Mi.ir) + i (Mi.rr + Mi.ii + Mr.ri - Mr.ir)
+__global__ void assemble_kernel(const double *__restrict__ M64, int Mp, int Gp, int ng, int nen,
+                                double2 *__restrict__ chi) {
+  const int e = blockIdx.y;
+  const double *Mr = M64 + ((size_t)e * 2 + 0) * Mp * Mp, *Mi = M64 + ((size_t)e * 2 + 1) * Mp * Mp;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (size_t)ng * ng;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(idx % ng), h = (int)(idx / ng);
+    const double rr_r = mget(Mr, Mp, g, h), ii_r = mget(Mr, Mp, Gp + g, Gp + h);
+    const double ri_r = mget(Mr, Mp, g, Gp + h), ir_r = mget(Mr, Mp, Gp + g, h);
+    const double rr_i = mget(Mi, Mp, g, h), ii_i = mget(Mi, Mp, Gp + g, Gp + h);
+    const double ri_i = mget(Mi, Mp, g, Gp + h), ir_i = mget(Mi, Mp, Gp + g, h);
+    double2 *d = chi + (size_t)e * ng * ng + idx;
+    d->x += rr_r + ii_r - ri_i + ir_i;
+    d->y += rr_i + ii_i + ri_r - ir_r;
+  }
+}
+
+}  // namespace
+
+void TcWorkspace::release() {
+  if (planes) cudaFree(planes);
+  if (part) cudaFree(part);
+  planes = part = nullptr;
+  planes_bytes = part_bytes = 0;
+}
+
+static void *grow(void *&p, size_t &have, size_t need) {
+  if (need <= have) return p;
+  if (p) cudaFree(p);
+  p = nullptr;
+  have = 0;
+  RP_CUDA(cudaMalloc(&p, need));
+  have = need;
+  return p;
+}
+
+static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
+
+void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st) {
+  ws.ng = ng; ws.nen = nen; ws.ndir = ndir;
+  const int Mp = 2 * Gp_of(ng);
+  const size_t mbytes = sizeof(double) * (size_t)nen * 2 * Mp * Mp;
+  grow(ws.part, ws.part_bytes, mbytes);
+  RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
+}
+
+int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *w, const double2 *head, int npair, int ntk,
+                      int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol, int *err,
+                      cudaStream_t st) {
+  (void)chi;
+  if (npair == 0) return 0;
+  int launches = 0;
+  const int Gp = Gp_of(ng), Mp = 2 * Gp;
+  const long Kn = (long)npair * ntk;
+  const int Kp = (int)(((Kn + BK - 1) / BK) * BK);
+  // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float2, maxes
+  const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float2) * (size_t)nen * Kp;
+  const size_t mxbytes = sizeof(float) * (1 + 2 * (size_t)nen);
+  unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, ybytes + wbytes + mxbytes + 256);
+  float *Yt = (float *)base;
+  float2 *wt = (float2 *)(base + ybytes);
+  float *maxes = (float *)(base + ybytes + wbytes);
+  RP_CUDA(cudaMemsetAsync(base, 0, ybytes + wbytes + mxbytes, st));
+  if (Kn > 0x7fffffffL) fail(1, "batch too large");
+  yt_kernel<<<(unsigned)Kn, 128, 0, st>>>(rho, npair, ntk, ng, Gp, Kp, Yt, head, g0);
+  wt_kernel<<<(unsigned)((Kn + 255) / 256), 256, 0, st>>>(w, npair, ntk, nen, Kp, wt);
+  maxes_kernel<<<1024, 256, 0, st>>>(Yt, (size_t)Mp * Kp, wt, nen, Kp, Kn, maxes);
+  launches += 3;
+  RP_CUDA(cudaGetLastError());
+  if (head && rowcol) {
+    dim3 g(ng, nen, 2);
+    gamma_rowcol_f32_kernel<<<g, 256, 0, st>>>(rho, w, head, npair, ntk, ng, nen, g0, rowcol);
+    launches++;
+    RP_CUDA(cudaGetLastError());
+  }
+  // upper tiles of the symmetric Gram matrix
+  const int nt = Mp / BM;
+  std::vector<int2> tl;
+  for (int i = 0; i < nt; i++)
+    for (int j = i; j < nt; j++) tl.push_back(make_int2(i, j));
+  static thread_local void *d_tiles = nullptr;
+  static thread_local size_t d_tiles_bytes = 0;
+  grow(d_tiles, d_tiles_bytes, sizeof(int2) * tl.size());
+  RP_CUDA(cudaMemcpyAsync(d_tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, st));
+  TcArgs a;
+  a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.M64 = (double *)ws.part; a.err = err;
+  a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;
+  a.nplanes = precision == RP_PREC_BF16X3 ? 3 : 2;
+  a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
+  a.ksub_blocks = 16;  // 1024 K per FP32 sub-chunk
+  a.tiles = (const int2 *)d_tiles;
+  const int tiles_per_stage = 3 * a.nplanes;
+  const size_t smem = 1024 + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES + 128;
+  if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
+  RP_CUDA(cudaFuncSetAttribute(tc_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)tl.size(), nen);
+  tc_gram_kernel<<<grid, NTHREADS, smem, st>>>(a);
+  launches++;
+  RP_CUDA(cudaGetLastError());
+  RP_CUDA(cudaStreamSynchronize(st));  // the workspace (and tile list) is reused by the next batch
+  return launches;
+}
+
+int tc_end_q(TcWorkspace &ws, double2 *chi, double2 *rowcol, cudaStream_t st) {
+  (void)rowcol;
+  const int Gp = Gp_of(ws.ng), Mp = 2 * Gp;
+  dim3 grid((unsigned)std::min<size_t>(((size_t)ws.ng * ws.ng + 255) / 256, 2048), ws.nen);
+  assemble_kernel<<<grid, 256, 0, st>>>((const double *)ws.part, Mp, Gp, ws.ng, ws.nen, chi);
+  RP_CUDA(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace rp

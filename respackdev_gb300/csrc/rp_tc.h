@@ -1,0 +1,28 @@
+// rp_tc.h -- tensor-core (tcgen05) chi0 contraction with split-precision operands.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace rp {
+
+// Device scratch of the tensor-core contraction (operand planes, FP32 partials).
+struct TcWorkspace {
+  void *planes = nullptr;
+  size_t planes_bytes = 0;
+  void *part = nullptr;
+  size_t part_bytes = 0;
+  int ng = 0, nen = 0, ndir = 1;
+  size_t bytes() const { return planes_bytes + part_bytes; }
+  void release();
+};
+
+void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st);
+// Adds the batch's contribution to chi (FP64, [dir][e][g + ng g']) and, at
+// Gamma, to the G=0 rows/columns of directions 2 and 3 (rowcol).
+int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *w, const double2 *head, int npair, int ntk,
+                      int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol, int *err,
+                      cudaStream_t st);
+int tc_end_q(TcWorkspace &ws, double2 *chi, double2 *rowcol, cudaStream_t st);
+
+}  // namespace rp

@@ -1,0 +1,433 @@
+// rp_tetra.cu -- generalized tetrahedron weights in FP64 (K4), built with
+// --fmad=false so the closed forms round like the reference's.
+//
+// Follows src/chiqw/m_tetrahedron_20170325.F (MIT-licensed Fujiwara et al.
+// generalized tetrahedron method): ttrhdrn_chi0 (:99-141) splits every
+// tetrahedron of the k mesh at the Fermi level (ttct, :143-207), classifies
+// near-degenerate vertex energies (chk1, :457-503) and evaluates the closed
+// forms (:304-451) per frequency, scattering them to the four vertices (calc,
+// :209-302).  chiqw.F:1371-1383 calls it for dsgn = +1 and -1 with the pair's
+// energies rounded to single precision (kindless CMPLX, chiqw.F:1354,1357).
+//
+// One CTA per (band pair, frequency chunk).  The weights of the chunk live in
+// shared memory (ntk x nchunk complex) and every thread walks tetrahedra,
+// adding its vertex terms with shared-memory FP64 atomics.  Tetrahedra that the
+// Fermi level does not cut (all of them for an insulator) skip ttct.
+#include "rp_dev.cuh"
+#include "rp_host.h"
+
+namespace rp {
+
+struct cx {
+  double r, i;
+  __device__ cx() : r(0), i(0) {}
+  __device__ cx(double a, double b = 0) : r(a), i(b) {}
+};
+__device__ __forceinline__ cx operator+(cx a, cx b) { return cx(a.r + b.r, a.i + b.i); }
+__device__ __forceinline__ cx operator-(cx a, cx b) { return cx(a.r - b.r, a.i - b.i); }
+__device__ __forceinline__ cx operator-(cx a) { return cx(-a.r, -a.i); }
+__device__ __forceinline__ cx operator*(cx a, cx b) { return cx(a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r); }
+__device__ __forceinline__ cx operator*(cx a, double s) { return cx(a.r * s, a.i * s); }
+__device__ __forceinline__ cx operator*(double s, cx a) { return cx(a.r * s, a.i * s); }
+__device__ __forceinline__ cx operator/(cx a, cx b) {
+  // Smith's algorithm
+  if (fabs(b.r) >= fabs(b.i)) {
+    double t = b.i / b.r, d = b.r + b.i * t;
+    return cx((a.r + a.i * t) / d, (a.i - a.r * t) / d);
+  }
+  double t = b.r / b.i, d = b.r * t + b.i;
+  return cx((a.r * t + a.i) / d, (a.i * t - a.r) / d);
+}
+__device__ __forceinline__ cx operator/(cx a, double s) { return cx(a.r / s, a.i / s); }
+__device__ __forceinline__ cx operator/(double s, cx b) { return cx(s, 0) / b; }
+__device__ __forceinline__ double cabs_(cx a) { return hypot(a.r, a.i); }
+__device__ __forceinline__ cx clog_(cx a) { return cx(log(hypot(a.r, a.i)), atan2(a.i, a.r)); }
+
+// ---- closed forms (m_tetrahedron_20170325.F:304-451), one frequency w ----
+__device__ cx s1g30g21(cx g0, cx g1, cx w) {
+  cx d = g0 - g1;
+  cx v = (0.5 * (g0 + g1) + w) / (d * d);
+  return v - clog_((g0 + w) / (g1 + w)) * (g0 + w) * (g1 + w) / (d * d * d);
+}
+__device__ cx s1g30g20(cx g0, cx g1, cx w) {
+  cx d = g0 - g1;
+  cx v = (g0 - 3.0 * g1 - 2.0 * w) * 0.25 / (d * d);
+  return v + (g1 + w) * (g1 + w) * clog_((g0 + w) / (g1 + w)) * 0.5 / (d * d * d);
+}
+__device__ cx s1g30(cx g0, cx g1, cx g2, cx w) {
+  cx v = 0.5 / (g0 - g2);
+  cx t = (g0 - g2) * (g0 - g1);
+  v = v - 0.5 / (t * t) * (g0 + w) * (-2.0 * (g1 + w) * (g2 + w) + (g0 + w) * (g1 + g2 + 2.0 * w)) *
+              clog_((g0 + w) / (g1 + w));
+  v = v + 0.5 / ((g0 - g2) * (g0 - g2)) * (g2 + w) * (g2 + w) * clog_((g1 + w) / (g2 + w)) / (g1 - g2);
+  return v + 0.5 / ((g0 - g2) * (g0 - g1)) * (g1 + w);
+}
+__device__ cx s1normal(cx g0, cx g1, cx g2, cx g3, cx w) {
+  cx L10 = clog_((g1 + w) / (g0 + w)), L20 = clog_((g2 + w) / (g0 + w)), L30 = clog_((g3 + w) / (g0 + w));
+  cx v = (-(g1 + w) * (g1 + w) * L10) / ((g0 - g2) * (g0 - g3) * (g0 - g1)) * 0.5;
+  v = v - ((g1 + w) * (g1 + w) * L10 - (g2 + w) * (g2 + w) * L20) / ((g0 - g2) * (g1 - g2) * (g2 - g3)) * 0.5;
+  return v + ((g1 + w) * (g1 + w) * L10 - (g3 + w) * (g3 + w) * L30) / ((g1 - g3) * (g0 - g3) * (g2 - g3)) * 0.5;
+}
+__device__ cx s2simple(cx g0, cx w) { return 1.0 / ((g0 + w) * 24.0); }
+__device__ cx s2g30g20(cx g0, cx g1, cx w) {
+  cx d = g0 - g1;
+  cx v = ((g0 - g1) * (g0 + 2.0 * g1 + 3.0 * w) - 6.0 * (g0 + w) * (g1 + w)) / (12.0 * (d * d * d));
+  return v + (g0 + w) * (g1 + w) * (g1 + w) * clog_((g0 + w) / (g1 + w)) / (d * d * d * d) * 0.5;
+}
+__device__ cx s2g30g10(cx g0, cx g2, cx w) {
+  cx d = g0 - g2;
+  cx v = (2.0 * (g0 + w) * (g0 + w) - 7.0 * (g0 + w) * (g2 + w) + 11.0 * (g2 + w) * (g2 + w)) / (36.0 * (d * d * d));
+  return v - (g2 + w) * (g2 + w) * (g2 + w) * clog_((g0 + w) / (g2 + w)) / (6.0 * (d * d * d * d));
+}
+__device__ cx s2g10(cx g0, cx g2, cx g3, cx w) {
+  cx d2 = g0 - g2, d3 = g0 - g3;
+  cx v = (g0 + w) * ((g0 + w) * (g0 + w) + 5.0 * (g2 + w) * (g3 + w) - 3.0 * (g0 + w) * (g2 + g3 + 2.0 * w)) /
+         (12.0 * (d2 * d2) * (d3 * d3));
+  v = v - (g2 + w) * (g2 + w) * (g2 + w) * clog_((g2 + w) / (g0 + w)) / (6.0 * (d2 * d2 * d2) * (g2 - g3));
+  return v + (g3 + w) * (g3 + w) * (g3 + w) * clog_((g3 + w) / (g0 + w)) / (6.0 * (d3 * d3 * d3) * (g2 - g3));
+}
+__device__ cx s2g30(cx g0, cx g1, cx g2, cx w) {
+  cx d01 = g0 - g1, d02 = g0 - g2, d12 = g1 - g2;
+  cx v = ((g0 + w) * (g0 + w) * (g1 - g2) + (g1 + w) * (g1 + w) * (g0 - g2)) / (6.0 * d02 * (d01 * d01) * d12);
+  v = v - (g0 + w) * (g0 + w) * (2.0 * (g1 + w) * (g0 - g2) + (g2 + w) * (g0 - g1)) * clog_((g0 + w) / (g2 + w)) /
+              (6.0 * (d02 * d02) * (d01 * d01 * d01));
+  return v + (g1 + w) * (g1 + w) * (2.0 * (g0 + w) * (g1 - g2) - (g2 + w) * (g0 - g1)) * clog_((g1 + w) / (g2 + w)) /
+                 (6.0 * (d01 * d01 * d01) * (d12 * d12));
+}
+__device__ cx s2normal(cx g0, cx g1, cx g2, cx g3, cx w) {
+  cx v = -(g1 + w) * (g1 + w) / (6.0 * (g0 - g1) * (g1 - g2) * (g1 - g3));
+  v = v - (g2 + w) * (g2 + w) * (g2 + w) * clog_((g2 + w) / (g1 + w)) / (6.0 * (g0 - g2) * ((g1 - g2) * (g1 - g2)) * (g2 - g3));
+  v = v + (g3 + w) * (g3 + w) * (g3 + w) * clog_((g3 + w) / (g1 + w)) / (6.0 * (g0 - g3) * ((g1 - g3) * (g1 - g3)) * (g2 - g3));
+  return v + (g0 + w) * (g0 + w) * (g0 + w) * clog_((g0 + w) / (g1 + w)) / (6.0 * ((g0 - g1) * (g0 - g1)) * (g0 - g2) * (g0 - g3));
+}
+
+// chk1 on positions 0..3 (ia1 = identity); returns case (sum ia2) and i3
+struct Chk { int s, i3; int ia3[4], ia4[4]; };
+__device__ Chk chk1(double dmna, double dmnr, const cx *gk) {
+  Chk c;
+  int ia2[4] = {0, 0, 0, 0}, i3 = 0, i4 = 0;
+  for (int a = 0; a < 4; a++) { c.ia3[a] = 0; c.ia4[a] = 0; }
+  for (int i1 = 1; i1 <= 3; i1++)
+    for (int i2 = i1 + 1; i2 <= 4; i2++) {
+      int p = i1 % 4, r = i2 % 4;
+      double d1 = cabs_(gk[p] - gk[r]);
+      double d2 = cabs_(gk[p] + gk[r]) * 0.5;
+      if (d1 < dmna || d1 / d2 < dmnr) {
+        i3++;
+        if (ia2[p] == 0) { c.ia3[i4++] = p; ia2[p] = 1; }
+        if (ia2[r] == 0) { c.ia3[i4++] = r; ia2[r] = 1; }
+      }
+    }
+  int i5 = 0;
+  for (int i1 = 1; i1 <= 4; i1++) { int p = i1 % 4; if (ia2[p] == 0) c.ia4[i5++] = p; }
+  c.s = ia2[0] + ia2[1] + ia2[2] + ia2[3];
+  c.i3 = i3;
+  return c;
+}
+
+// calc() for one frequency: vertex terms x[0..3] (positions), fk per position
+__device__ bool calc_w(const Chk &c, const cx *fk, const cx *gk, cx w, cx *x) {
+  x[0] = x[1] = x[2] = x[3] = cx(0, 0);
+  switch (c.s) {
+  case 0: {
+    const int *a = c.ia4;
+    cx c1 = s2normal(gk[a[1]], gk[a[0]], gk[a[2]], gk[a[3]], w);
+    cx c2 = s2normal(gk[a[0]], gk[a[1]], gk[a[2]], gk[a[3]], w);
+    cx c3 = s2normal(gk[a[0]], gk[a[2]], gk[a[1]], gk[a[3]], w);
+    cx c4 = s1normal(gk[a[0]], gk[a[3]], gk[a[1]], gk[a[2]], w);
+    x[a[0]] = fk[a[0]] * c1;
+    x[a[1]] = fk[a[1]] * c2;
+    x[a[2]] = fk[a[2]] * c3;
+    x[a[3]] = fk[a[3]] * (c4 - c3 - c2 - c1);
+    return true;
+  }
+  case 2: {
+    cx geq1 = (gk[c.ia3[0]] + gk[c.ia3[1]]) / 2.0;
+    cx c1 = s2g10(geq1, gk[c.ia4[0]], gk[c.ia4[1]], w);
+    cx c2 = s2g30(geq1, gk[c.ia4[0]], gk[c.ia4[1]], w);
+    cx c3 = s1g30(geq1, gk[c.ia4[1]], gk[c.ia4[0]], w);
+    x[c.ia3[0]] = fk[c.ia3[0]] * c1;
+    x[c.ia3[1]] = fk[c.ia3[1]] * c1;
+    x[c.ia4[0]] = fk[c.ia4[0]] * c2;
+    x[c.ia4[1]] = fk[c.ia4[1]] * (c3 - c2 - c1 - c1);
+    return true;
+  }
+  case 3: {
+    cx geq1 = (gk[c.ia3[0]] + gk[c.ia3[1]] + gk[c.ia3[2]]) / 3.0;
+    cx c1 = s2g30g10(geq1, gk[c.ia4[0]], w);
+    cx c2 = s1g30g20(geq1, gk[c.ia4[0]], w);
+    x[c.ia3[0]] = fk[c.ia3[0]] * c1;
+    x[c.ia3[1]] = fk[c.ia3[1]] * c1;
+    x[c.ia3[2]] = fk[c.ia3[2]] * c1;
+    x[c.ia4[0]] = fk[c.ia4[0]] * (c2 - c1 - c1 - c1);
+    return true;
+  }
+  case 4:
+    if (c.i3 == 2) {
+      cx geq1 = (gk[c.ia3[0]] + gk[c.ia3[1]]) / 2.0, geq2 = (gk[c.ia3[2]] + gk[c.ia3[3]]) / 2.0;
+      cx c1 = s2g30g20(geq1, geq2, w);  // ttrhdrn_sub2g30g21(geq2,geq1,...) = sub2g30g20(geq1,geq2)
+      cx c2 = s1g30g21(geq1, geq2, w);
+      x[c.ia3[0]] = fk[c.ia3[0]] * c1;
+      x[c.ia3[1]] = fk[c.ia3[1]] * c1;
+      x[c.ia3[2]] = fk[c.ia3[2]] * (c2 - c1 - c1) * 0.5;
+      x[c.ia3[3]] = fk[c.ia3[3]] * (c2 - c1 - c1) * 0.5;
+      return true;
+    } else if (c.i3 >= 3 && c.i3 <= 6) {
+      cx geq1 = (gk[c.ia3[0]] + gk[c.ia3[1]] + gk[c.ia3[2]] + gk[c.ia3[3]]) / 4.0;
+      cx c1 = s2simple(geq1, w);
+      for (int a = 0; a < 4; a++) x[c.ia3[a]] = c1 * fk[c.ia3[a]];
+      return true;
+    }
+    return false;
+  default:
+    return false;
+  }
+}
+
+#define TT_NMAX 64
+
+// ttct (:143-207) on local arrays; returns false when more than TT_NMAX pieces
+__device__ bool ttct(double dval, const double *dvtx, int imod, int &ntet, double (*dwgt)[4][4], double *dvol) {
+  unsigned char bvtx[TT_NMAX][4];
+  bool btsk[TT_NMAX];
+  for (int t = 0; t < TT_NMAX; t++) { btsk[t] = false; bvtx[t][0] = bvtx[t][1] = bvtx[t][2] = bvtx[t][3] = 0; }
+  int itet = 0;
+  while (itet < ntet) {
+    itet++;
+    const int t = itet - 1;
+    double d0[4];
+    for (int i1 = 0; i1 < 4; i1++) {
+      double s = 0;
+      for (int v = 0; v < 4; v++) s += dwgt[t][i1][v] * dvtx[v];
+      d0[i1] = s;
+    }
+    bool b1 = false;
+    int i1, i2 = 0;
+    for (i1 = 0; i1 < 3; i1++) {
+      if (bvtx[t][i1]) continue;
+      for (i2 = i1 + 1; i2 < 4; i2++) {
+        if (bvtx[t][i2]) continue;
+        b1 = (d0[i1] - dval) * (dval - d0[i2]) > 0.0;
+        if (b1) break;
+      }
+      if (b1) break;
+    }
+    if (b1) {
+      double dd1 = (d0[i2] - dval) / (d0[i2] - d0[i1]);
+      double dd2 = (dval - d0[i1]) / (d0[i2] - d0[i1]);
+      ntet++;
+      if (ntet > TT_NMAX) return false;
+      const int nt = ntet - 1;
+      for (int a = 0; a < 4; a++) {
+        bvtx[nt][a] = bvtx[t][a];
+        for (int v = 0; v < 4; v++) dwgt[nt][a][v] = dwgt[t][a][v];
+      }
+      bvtx[nt][i1] = 1;
+      for (int v = 0; v < 4; v++) dwgt[nt][i1][v] = dwgt[t][i1][v] * dd1 + dwgt[t][i2][v] * dd2;
+      dvol[nt] = dvol[t] * dd1;
+      bvtx[t][i2] = 1;
+      for (int v = 0; v < 4; v++) dwgt[t][i2][v] = dwgt[t][i1][v] * dd1 + dwgt[t][i2][v] * dd2;
+      dvol[t] = dvol[t] * dd2;
+      itet--;
+    } else {
+      for (int a = 0; a < 4; a++) {
+        if (bvtx[t][a]) continue;
+        btsk[t] = btsk[t] || ((double)imod * (d0[a] - dval) > 0.0);
+      }
+    }
+  }
+  int k = 0;
+  for (int a = 0; a < ntet; a++) {
+    if (!btsk[a]) continue;
+    for (int i = 0; i < 4; i++)
+      for (int v = 0; v < 4; v++) dwgt[k][i][v] = dwgt[a][i][v];
+    dvol[k] = dvol[a];
+    k++;
+  }
+  ntet = k;
+  return true;
+}
+
+__device__ __forceinline__ void sadd(double2 *xo, cx v) {
+  atomicAdd(&xo->x, v.r);
+  atomicAdd(&xo->y, v.i);
+}
+
+// one (sub)tetrahedron: add its terms for frequencies [e0, e0+ne) into xo[slot*stride + e]
+__device__ bool tetra_terms(double dmna, double dmnr, const cx *ffk, const cx *ggk, const double2 *em, int e0,
+                            int ne, int stride, const int *slot, const double (*wgt)[4], double2 *xo) {
+  Chk c = chk1(dmna, dmnr, ggk);
+  for (int e = 0; e < ne; e++) {
+    cx w(em[e0 + e].x, em[e0 + e].y);
+    cx x[4];
+    if (!calc_w(c, ffk, ggk, w, x)) return false;
+    if (wgt == nullptr) {
+      for (int a = 0; a < 4; a++) sadd(&xo[slot[a] * stride + e], x[a]);
+    } else {
+      for (int i5 = 0; i5 < 4; i5++) {
+        cx s = x[0] * wgt[0][i5] + x[1] * wgt[1][i5] + x[2] * wgt[2][i5] + x[3] * wgt[3][i5];
+        sadd(&xo[slot[i5] * stride + e], s);
+      }
+    }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec, double2 *__restrict__ wout) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int p = blockIdx.x, e0 = blockIdx.y * nec, ntk = a.ntk;
+  const int ne = min(nec, a.nen - e0);
+  double2 *xo = (double2 *)smem;               // ntk * nec
+  double *e1m = (double *)(xo + (size_t)ntk * nec), *e2m = e1m + ntk;
+  const int bv = a.pair_vir[p], bo = a.pair_occ[p];
+  for (int i = threadIdx.x; i < ntk * nec; i += blockDim.x) xo[i] = make_double2(0, 0);
+  for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
+    int k = a.index_kpt[m];
+    e1m[m] = (double)(float)a.energy[(size_t)a.numirr[k] * a.ntb + bo];
+    e2m[m] = (double)(float)a.energy[(size_t)a.numirr[a.kpq[k]] * a.ntb + bv];
+  }
+  __syncthreads();
+  const double f = a.efermi, delt = a.delt;
+  for (int t = threadIdx.x; t < 6 * ntk; t += blockDim.x) {
+    int slot[4];
+    double ee1[4], ee2[4];
+    for (int v = 0; v < 4; v++) { slot[v] = a.imt1[4 * t + v]; ee1[v] = e1m[slot[v]]; ee2[v] = e2m[slot[v]]; }
+    double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
+    double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
+    double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
+    if (mx2 <= f) continue;  // ttct(+1) drops the whole tetrahedron
+    for (int sg = 0; sg < 2; sg++) {
+      const double dsgn = sg == 0 ? 1.0 : -1.0;
+      if (mn2 > f && mx1 < f) {
+        // not cut: one piece, identity weights, volume 1
+        cx ffk[4], ggk[4];
+        for (int v = 0; v < 4; v++) {
+          ffk[v] = cx(dsgn, 0);
+          ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
+        }
+        if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, nullptr, xo)) atomicExch(a.err, 2);
+        continue;
+      }
+      double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
+      for (int i = 0; i < 4; i++)
+        for (int v = 0; v < 4; v++) dwgt[0][i][v] = (i == v) ? 1.0 : 0.0;
+      dvol[0] = 1.0;
+      int ntet = 1;
+      if (!ttct(f, ee2, +1, ntet, dwgt, dvol) || !ttct(f, ee1, -1, ntet, dwgt, dvol)) { atomicExch(a.err, 1); continue; }
+      for (int i3 = 0; i3 < ntet; i3++) {
+        cx ffk[4], ggk[4];
+        for (int i4 = 0; i4 < 4; i4++) {
+          double s = 0;
+          for (int v = 0; v < 4; v++) s += (ee2[v] - ee1[v]) * dwgt[i3][i4][v];
+          ffk[i4] = cx(dvol[i3], 0) * dsgn;
+          ggk[i4] = cx(-s, delt) * dsgn;
+        }
+        double w4[4][4];
+        for (int i4 = 0; i4 < 4; i4++)
+          for (int v = 0; v < 4; v++) w4[i4][v] = dwgt[i3][i4][v];
+        if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, w4, xo)) atomicExch(a.err, 2);
+      }
+    }
+  }
+  __syncthreads();
+  // w[(p*nen + e)*ntk + k] = xow(mesh(k), e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
+  for (int i = threadIdx.x; i < ntk * ne; i += blockDim.x) {
+    const int e = i / ntk, k = i % ntk;
+    int m = 0;
+    // mesh slot of k: index_kpt is a permutation; invert it via a scan-free lookup
+    m = a.index_kpt[ntk + k];  // second half holds the inverse map
+    double2 x = xo[(size_t)m * nec + e];
+    double2 po = a.prob[(size_t)k * a.ntb + bo], pv = a.prob[(size_t)a.kpq[k] * a.ntb + bv];
+    double2 pp = make_double2(1.0 - (po.x * pv.x - po.y * pv.y), -(po.x * pv.y + po.y * pv.x));
+    double2 r = cmul(x, pp);
+    wout[((size_t)p * a.nen + e0 + e) * ntk + k] = make_double2(r.x / (double)ntk, r.y / (double)ntk);
+  }
+}
+
+int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st) {
+  if (a.npair == 0) return 0;
+  int nec = a.nen;
+  const size_t budget = 180 * 1024 - 16 * (size_t)a.ntk;
+  while (nec > 1 && (size_t)a.ntk * nec * sizeof(double2) > budget) nec = (nec + 1) / 2;
+  size_t smem = (size_t)a.ntk * nec * sizeof(double2) + 2 * sizeof(double) * a.ntk;
+  if (smem > 227 * 1024) fail(1, "k mesh too large for the tetrahedron tile (%zu bytes)", smem);
+  RP_CUDA(cudaFuncSetAttribute(tetra_weights_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(a.npair, (a.nen + nec - 1) / nec);
+  tetra_weights_kernel<<<grid, 256, smem, st>>>(a, nec, w);
+  RP_CUDA(cudaGetLastError());
+  return 1;
+}
+
+// ---------------------------------------------------------------------------
+// Intraband plasma frequency at Gamma for metals (chiqw.F:1639-1733): for each
+// partially occupied band b, pk(k) = sum_G (k+G) |C_b(k,G)|^2 (calc_VMaa) and
+// xo = ttrhdrn_simple(fk=1, gk = E_b(k) - E_F - i delt) at w = 0;
+// pwpl += Im(xo) pk^2.
+__global__ void __launch_bounds__(256) intraband_kernel(TetraArgs a, const double2 *__restrict__ cfull,
+                                                        const int *__restrict__ ng0, const int *__restrict__ kg0,
+                                                        int ncb, int ntg, const double *__restrict__ b9,
+                                                        const double *__restrict__ sk0, const int *__restrict__ bands,
+                                                        double2 *__restrict__ pwpl) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ntk = a.ntk, b = bands[blockIdx.x];
+  double2 *xo = (double2 *)smem;           // ntk (mesh slots)
+  double *pk = (double *)(xo + ntk);       // 3*ntk (by k)
+  cx *gk = (cx *)(pk + 3 * ntk);           // ntk (mesh slots)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
+    xo[m] = make_double2(0, 0);
+    int k = a.index_kpt[m];
+    double e = a.energy[(size_t)a.numirr[k] * a.ntb + b] - a.efermi;
+    gk[m] = cx((double)(float)e, (double)(float)(-a.delt));
+  }
+  for (int k = warp; k < ntk; k += nw) {
+    double s[3] = {0, 0, 0};
+    const double2 *c = cfull + ((size_t)k * ncb + b) * ntg;
+    for (int ig = lane; ig < ng0[k]; ig += 32) {
+      const int *g = kg0 + ((size_t)k * ntg + ig) * 3;
+      double w = c[ig].x * c[ig].x + c[ig].y * c[ig].y;
+      for (int d = 0; d < 3; d++) {
+        double G = (sk0[3 * k] + g[0]) * b9[d] + (sk0[3 * k + 1] + g[1]) * b9[3 + d] + (sk0[3 * k + 2] + g[2]) * b9[6 + d];
+        s[d] += G * w;
+      }
+    }
+    for (int d = 0; d < 3; d++)
+      for (int o = 16; o; o >>= 1) s[d] += __shfl_xor_sync(0xffffffffu, s[d], o);
+    if (lane == 0)
+      for (int d = 0; d < 3; d++) pk[3 * k + d] = s[d];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < 6 * ntk; t += blockDim.x) {
+    int slot[4];
+    cx ffk[4], ggk[4];
+    for (int v = 0; v < 4; v++) { slot[v] = a.imt1[4 * t + v]; ffk[v] = cx(1, 0); ggk[v] = gk[slot[v]]; }
+    Chk c = chk1(a.dmna, a.dmnr, ggk);
+    cx x[4];
+    if (!calc_w(c, ffk, ggk, cx(0, 0), x)) { atomicExch(a.err, 2); continue; }
+    for (int v = 0; v < 4; v++) sadd(&xo[slot[v]], x[v]);
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    const int d = threadIdx.x;
+    double s = 0;
+    for (int m = 0; m < ntk; m++) {
+      int k = a.index_kpt[m];
+      s += xo[m].y * pk[3 * k + d] * pk[3 * k + d];
+    }
+    atomicAdd(&pwpl[d].x, s);
+  }
+}
+
+int launch_intraband(const TetraArgs &a, const double2 *cfull, const int *ng0, const int *kg0, int ncb, int ntg,
+                     const double *bvec9, const double *sk0, const int *bands, int nb, double2 *pwpl,
+                     cudaStream_t st) {
+  if (nb == 0) return 0;
+  size_t smem = (size_t)a.ntk * (sizeof(double2) + 3 * sizeof(double) + sizeof(cx));
+  if (smem > 227 * 1024) fail(1, "k mesh too large for the intraband tile");
+  RP_CUDA(cudaFuncSetAttribute(intraband_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  intraband_kernel<<<nb, 256, smem, st>>>(a, cfull, ng0, kg0, ncb, ntg, bvec9, sk0, bands, pwpl);
+  RP_CUDA(cudaGetLastError());
+  return 1;
+}
+
+}  // namespace rp

@@ -1,0 +1,67 @@
+"""Shared helpers of the parity tests."""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from respackdev_gb300 import synth
+
+AU = 27.21151
+
+# frequencies used by the parity runs (explicit grid, Hartree): real 0-10 eV and
+# one complex point
+EM_TEST = np.array([0.0, 1.5, 4.0, 10.0], dtype=np.complex128) / AU
+EM_TEST = np.concatenate([EM_TEST, [0.5j / AU]])
+
+
+def normwise_err(a: np.ndarray, b: np.ndarray) -> float:
+    """max over frequencies/directions of max|a-b| / max|b| (per frequency slice)."""
+    a = a.reshape(a.shape[0], a.shape[1], -1)
+    b = b.reshape(b.shape[0], b.shape[1], -1)
+    worst = 0.0
+    for i in range(b.shape[2]):
+        den = np.abs(b[:, :, i]).max()
+        if den == 0:
+            continue
+        worst = max(worst, float(np.abs(a[:, :, i] - b[:, :, i]).max() / den))
+    return worst
+
+
+def run_params(case: str):
+    """Namelist values of the parity runs of a synthetic case."""
+    kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0)
+    if case == "tiny_metal_crpa":
+        kw["flg_crpa"] = 1
+    if case == "config1":
+        kw.update(ecut_for_eps=3.0, flg_crpa=1)
+    return kw
+
+
+def case_name(case: str) -> str:
+    return "tiny_metal" if case == "tiny_metal_crpa" else case
+
+
+def read_eps_record(path: str, ng: int, nen: int) -> np.ndarray:
+    rec = synth.read_unformatted_records(path)
+    assert len(rec) == 1
+    return np.frombuffer(rec[0], dtype=np.complex128).reshape(nen, ng, ng).transpose(2, 1, 0)
+
+
+def namelist_text(kw: dict, em=None, extra_gpu: str = "") -> str:
+    lines = ["&param_chiqw"]
+    names = {"green_func_delt": "Green_func_delt", "ecut_for_eps": "Ecut_for_eps", "flg_crpa": "flg_cRPA",
+             "n_calc_band": "N_CALC_BAND", "flg_calc_type": "flg_calc_type", "n_calc_q": "n_calc_q"}
+    for k, v in kw.items():
+        lines.append(f" {names.get(k, k)}={v}")
+    lines.append("/")
+    gpu = []
+    if em is not None:
+        em = np.asarray(em)
+        gpu.append("freq_re_ev=" + ",".join(f"{x:.17g}" for x in em.real * AU))
+        gpu.append("freq_im_ev=" + ",".join(f"{x:.17g}" for x in em.imag * AU))
+    if extra_gpu:
+        gpu.append(extra_gpu)
+    if gpu:
+        lines.append("&param_gpu " + ", ".join(gpu) + " /")
+    return "\n".join(lines) + "\n"
