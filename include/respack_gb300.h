@@ -24,7 +24,8 @@ enum rp_precision {
   RP_PREC_FP64 = 0,    /* plain FP64 everywhere (pair densities, contraction)      */
   RP_PREC_FP16X2 = 1,  /* FP32 pair densities; tcgen05 contraction, 2-term FP16
                           split (3 products), FP32 accumulate, FP64 chunk reduce  */
-  RP_PREC_BF16X3 = 2   /* as FP16X2 with a 3-term BF16 split (6 products)        */
+  RP_PREC_BF16X3 = 2,  /* as FP16X2 with a 3-term BF16 split (6 products)        */
+  RP_PREC_FP16X3 = 3   /* as FP16X2 with a 3-term FP16 split (6 products)        */
 };
 
 /* &param_chiqw (src/chiqw/m_rdinput.f90:41-45, defaults :52-73) in the
@@ -55,6 +56,10 @@ typedef struct rp_params {
   int    max_pairs;            /* >0: keep only the first pairs (timing)     */
   int    qshard_index;         /* this process's shard of the q list        */
   int    qshard_count;         /* number of shards (1 = all q here)          */
+  int    pair_fp64;            /* tensor-core precisions: pair densities in FP64
+                                  (as the reference) instead of FP32          */
+  int    tc_ksub;              /* K blocks (of 64) per FP32 accumulation before
+                                  the FP64 reduction (0 = default)            */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */

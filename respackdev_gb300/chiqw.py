@@ -18,7 +18,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
-PREC_FP64, PREC_FP16X2, PREC_BF16X3 = 0, 1, 2
+PREC_FP64, PREC_FP16X2, PREC_BF16X3, PREC_FP16X3 = 0, 1, 2, 3
 
 
 def library_path() -> str:
@@ -34,7 +34,7 @@ class Params(C.Structure):
         ("file_num_log_start", C.c_int), ("file_num_eps_start", C.c_int), ("file_num_eps_base_start", C.c_int),
         ("n_calc_q", C.c_int), ("mpi_num_qcomm", C.c_int), ("precision", C.c_int), ("fft_box", C.c_int * 3),
         ("dump_chi", C.c_int), ("device", C.c_int), ("max_pairs", C.c_int), ("qshard_index", C.c_int),
-        ("qshard_count", C.c_int),
+        ("qshard_count", C.c_int), ("pair_fp64", C.c_int), ("tc_ksub", C.c_int),
     ]
 
 

@@ -218,12 +218,15 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
     return elt * ((size_t)n1 + n2 + n3 + 2 * (size_t)n1 * n2 + (size_t)D1 * n2 + D1 * D2 + (size_t)j * ng) +
            sizeof(int) * ((size_t)D1 + D2 + ng);
   };
-  const size_t elt = fast ? sizeof(float) * 2 : sizeof(double) * 2;
+  const size_t elt = (fast && !S.params.pair_fp64) ? sizeof(float) * 2 : sizeof(double) * 2;
   while (jmax > 1 && smem_of(jmax, elt) > 220 * 1024) jmax--;
   if (smem_of(jmax, elt) > 220 * 1024) rp::fail(1, "dielectric sphere (NG=%d) too large for the pair-density tile", ng);
   float tms[4] = {0, 0, 0, 0};
   RP_CUDA(cudaEventRecord(c->ev[5], st));
-  if (fast) rp::tc_begin_q(c->tcw, ng, nen, c->ndir, st);
+  if (fast) {
+    c->tcw.ksub = S.params.tc_ksub;
+    rp::tc_begin_q(c->tcw, ng, nen, c->ndir, st);
+  }
   for (int p0 = 0; p0 < npair; p0 += bsz) {
     const int nb = std::min(bsz, npair - p0);
     std::vector<int> bv(t.pair_vir.begin() + p0, t.pair_vir.begin() + p0 + nb);
@@ -274,10 +277,16 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
       c->launches += rp::launch_contract_fp64(c->rho.as<double2>(), c->wts.as<double2>(), nb, ntk, ng, nen,
                                               c->chi.as<double2>(), st);
     } else {
-      c->rho.ensure(sizeof(float) * 2 * (size_t)nb * ntk * ng);
-      c->launches += rp::launch_pair_density_fp32(c->ur.as<float2>(), pg, pc, c->rho.as<float2>(), st);
+      const bool p64 = S.params.pair_fp64 != 0;
+      c->rho.ensure((p64 ? sizeof(cd) : sizeof(float) * 2) * (size_t)nb * ntk * ng);
+      if (p64) c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
+      else c->launches += rp::launch_pair_density_fp32(c->ur.as<float2>(), pg, pc, c->rho.as<float2>(), st);
       RP_CUDA(cudaEventRecord(c->ev[2], st));
-      c->launches += rp::tc_contract_batch(c->tcw, c->rho.as<float2>(), c->wts.as<double2>(),
+      if (p64 && t.gamma)
+        c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
+                                               ntk, ng, nen, t.no_g0, c->rowcol.as<double2>(), st);
+      c->launches += rp::tc_contract_batch(c->tcw, p64 ? nullptr : c->rho.as<float2>(),
+                                           p64 ? c->rho.as<double2>() : nullptr, c->wts.as<double2>(),
                                            t.gamma ? c->head.as<double2>() : nullptr, nb, ntk, ng, nen, t.no_g0,
                                            S.params.precision, c->chi.as<double2>(),
                                            t.gamma ? c->rowcol.as<double2>() : nullptr, c->errw.as<int>(), st);

@@ -274,6 +274,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
         if (s == "fp64") p->precision = RP_PREC_FP64;
         else if (s == "fp16x2") p->precision = RP_PREC_FP16X2;
         else if (s == "bf16x3") p->precision = RP_PREC_BF16X3;
+        else if (s == "fp16x3") p->precision = RP_PREC_FP16X3;
         else fail(1, "&param_gpu precision: unknown '%s'", s.c_str());
       } else if (k == "fft_box") {
         if (v.size() != 3) fail(1, "&param_gpu fft_box needs 3 integers");
@@ -283,6 +284,8 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "max_pairs") p->max_pairs = nl_int(v, k);
       else if (k == "qshard_index") p->qshard_index = nl_int(v, k);
       else if (k == "qshard_count") p->qshard_count = nl_int(v, k);
+      else if (k == "pair_fp64") p->pair_fp64 = nl_int(v, k);
+      else if (k == "tc_ksub") p->tc_ksub = nl_int(v, k);
       else if (k == "freq_re_ev") for (auto &x : v) fre.push_back(to_num(x));
       else if (k == "freq_im_ev") for (auto &x : v) fim.push_back(to_num(x));
       else fail(1, "namelist &param_gpu: unknown name '%s'", k.c_str());

@@ -8,13 +8,18 @@
 // (Mr, Mi: x = Re / Im of the weight; rr, ri, ir, ii: quadrants of M).  M is
 // symmetric, so only tiles on or above the diagonal are computed.
 //
-// Precision: each operand value v is split into two FP16 terms v = hi + lo
-// (RP_PREC_FP16X2: products hi.hi + hi.lo + lo.hi) or three BF16 terms
-// (RP_PREC_BF16X3: the six products with i + j <= 2), after scaling the batch
-// by powers of two so FP16 stays in range.  The tensor cores accumulate in
-// FP32 in tensor memory over a sub-chunk of K; the epilogue warps then add the
-// sub-chunk into an FP64 copy of the tile in global memory, so FP32 rounding
-// never sees more than one sub-chunk.
+// Precision.  Every row of both operands gets a power-of-two scale from its
+// largest value.  RP_PREC_FP16X2 splits a scaled value into two FP16 terms
+// (products hi.hi + hi.lo + lo.hi, about 22 bits).  The three-term variants
+// (RP_PREC_FP16X3, RP_PREC_BF16X3) make the leading term an integer of at most
+// 8 bits (row scale maps the row maximum to 128) and carry the remainder in two
+// 16-bit floating terms of the same row units, keeping the six products with
+// plane(A) + plane(B) <= 2.  The tensor core's FP32 accumulator does not round
+// to nearest, so the products of integer leading terms go to their own
+// accumulator: their partial sums are integers below 2^24 over a sub-chunk of
+// up to 1024 K and stay exact; the five correction products, about 2^-7
+// smaller, go to a second accumulator.  After each sub-chunk the epilogue
+// warps add both, times the rows' scales, into an FP64 copy of the tile.
 //
 // Kernel layout (one CTA per (frequency, upper tile)), 288 threads:
 //   warps 0-3  producers: read FP32 rho and the weights, scale, split and store
@@ -29,6 +34,9 @@
 // (bounded) for its own MMAs and frees tensor memory before returning.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+
+#include <algorithm>
+#include <vector>
 
 #include "rp_dev.cuh"
 #include "rp_host.h"
@@ -49,11 +57,15 @@ constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
 struct TcArgs {
   const float *Yt;        // [Mp][Kp] rows: Re rho (0..Gp), Im rho (Gp..2Gp)
-  const float2 *wt;       // [nen][Kp] weights
+  const float *sB;        // [Mp] row scales of the unweighted operand
+  const float *sA;        // [2 nen][Mp] row scales of the weighted operand per channel
+  int exact;              // 1: integer leading plane + separate accumulator
+  const float4 *wt;       // [nen][Kp] weights as float pairs (re_hi, re_lo, im_hi, im_lo)
   const float *maxes;     // [0] = max|Y|, [1 + 2e] = max|Re w_e|, [2 + 2e] = max|Im w_e|
   double *M64;            // [nen][2][Mp][Mp] FP64 tiles (upper triangle used)
   int *err;
   int Mp, Kp, nen, ntile_side, ksub_blocks, nplanes, bf16;
+  int nch;                // channels (Re / Im weight) per CTA: 2, or 1 (grid.y = 2 nen)
   const int2 *tiles;      // (ta, tb) list, ta <= tb
 };
 
@@ -132,18 +144,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
-// power-of-two scale that maps |v| <= vmax to <= 2^14
-__device__ __forceinline__ float scale_for(float vmax) {
+// power-of-two scale that maps |v| <= vmax below 2^top (m 2^e -> m 2^top)
+__device__ __forceinline__ float scale_for(float vmax, int top) {
   if (!(vmax > 0.f)) return 1.f;
   int e;
   frexpf(vmax, &e);  // vmax = m 2^e, m in [0.5, 1)
-  return ldexpf(1.f, 14 - e);
+  return ldexpf(1.f, top - e);
 }
 
-// split v into nplanes 16-bit terms (fp16 x2 or bf16 x3), returned as raw bits
-__device__ __forceinline__ void split16(float v, int nplanes, int bf16, uint16_t *t) {
+// split the float pair v + vl into nplanes 16-bit terms (fp16 or bf16), raw bits;
+// exact: the leading term is rint(v), an integer the 16-bit format holds exactly
+__device__ __forceinline__ void split16(float v, float vl, int nplanes, int bf16, int exact, uint16_t *t) {
   float r = v;
   for (int p = 0; p < nplanes; p++) {
+    if (p == 1) r = r + vl;  // the low word joins once the leading term is removed
+    if (p == 0 && exact) {
+      const float h = rintf(r);
+      t[0] = bf16 ? __bfloat16_as_ushort(__float2bfloat16_rn(h)) : __half_as_ushort(__float2half_rn(h));
+      r = r - h;
+      continue;
+    }
     if (bf16) {
       __nv_bfloat16 h = __float2bfloat16_rn(r);
       t[p] = __bfloat16_as_ushort(h);
@@ -166,7 +186,8 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   // 1024-align the operand area
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int np = a.nplanes;                       // 2 (fp16) or 3 (bf16)
-  const int tiles_per_stage = np + 2 * np;        // B planes + 2 channels x A planes
+  const int nch = a.nch;                          // 2 or 1
+  const int tiles_per_stage = np * (1 + nch);     // B planes + nch x A planes
   unsigned char *stage_base = smem;
   uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES);
   uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accempty = bars + 6, *fin = bars + 8;
@@ -174,7 +195,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   uint32_t *tmem_slot = (uint32_t *)(bars + 10);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int e = blockIdx.y;
+  // frequency e and the first channel handled here (channel 0 = Re weight, 1 = Im weight)
+  const int e = nch == 2 ? blockIdx.y : blockIdx.y >> 1;
+  const int ch0 = nch == 2 ? 0 : (blockIdx.y & 1);
   const int2 tt = a.tiles[blockIdx.x];
   const int ta = tt.x, tb = tt.y;
   const int nkb = a.Kp / BK;
@@ -199,53 +222,57 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  const float ymax = a.maxes[0];
-  const float sB = scale_for(ymax);
-  const float sA0 = scale_for(ymax * a.maxes[1 + 2 * e]);
-  const float sA1 = scale_for(ymax * a.maxes[2 + 2 * e]);
+  const int cbase = 2 * e + ch0;  // channel index of lc = 0
 
   if (warp < 4) {
     // ---------------- producers: one operand row per thread ----------------
     const int r = tid;  // 0..127
+    const float sB = a.sB[tb * BM + r];
+    float sA[2];
+    for (int lc = 0; lc < nch; lc++) sA[lc] = a.sA[(size_t)(cbase + lc) * a.Mp + ta * BM + r];
     const float *ya = a.Yt + (size_t)(ta * BM + r) * a.Kp;
     const float *yb = a.Yt + (size_t)(tb * BM + r) * a.Kp;
-    const float2 *wt = a.wt + (size_t)e * a.Kp;
+    const float4 *wt = a.wt + (size_t)e * a.Kp;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
       unsigned char *st = stage_base + (size_t)s * tiles_per_stage * TILE_BYTES;
       const int k0 = kb * BK;
 #pragma unroll 1
-      for (int c = 0; c < 8; c++) {  // 8 chunks of 8 K values
+      for (int c = 0; c < 8; c++) {  // 8 chunks of 8 K values (16 bytes of 16-bit values)
         const float4 *pa = (const float4 *)(ya + k0 + 8 * c), *pb = (const float4 *)(yb + k0 + 8 * c);
-        float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), b0 = __ldg(pb), b1 = __ldg(pb + 1);
-        float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-        uint16_t tb16[3][8], t0[3][8], t1[3][8];
+        const float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), b0 = __ldg(pb), b1 = __ldg(pb + 1);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        uint16_t tbv[3][8], tav[2][3][8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          const float2 w = __ldg(wt + k0 + 8 * c + j);
+          const float4 w = __ldg(wt + k0 + 8 * c + j);
+          const float wh[2] = {w.x, w.z}, wl[2] = {w.y, w.w};
           uint16_t t[3];
-          split16(bv[j] * sB, np, a.bf16, t);
-          for (int p = 0; p < np; p++) tb16[p][j] = t[p];
-          split16(av[j] * w.x * sA0, np, a.bf16, t);
-          for (int p = 0; p < np; p++) t0[p][j] = t[p];
-          split16(av[j] * w.y * sA1, np, a.bf16, t);
-          for (int p = 0; p < np; p++) t1[p][j] = t[p];
+          split16(bv[j] * sB, 0.f, np, a.bf16, a.exact, t);
+          for (int p = 0; p < np; p++) tbv[p][j] = t[p];
+          for (int lc = 0; lc < nch; lc++) {
+            // (wh + wl) * y * s as a float pair: exact head product, error-free remainder
+            const float xs = wh[ch0 + lc] * sA[lc], xl = wl[ch0 + lc] * sA[lc];
+            const float zh = xs * av[j];
+            const float zl = fmaf(xl, av[j], fmaf(xs, av[j], -zh));
+            split16(zh, zl, np, a.bf16, a.exact, t);
+            for (int p = 0; p < np; p++) tav[lc][p][j] = t[p];
+          }
         }
         const uint32_t off = swz(r, c);
         for (int p = 0; p < np; p++) {
-          uint4 vb, v0, v1;
-          vb.x = tb16[p][0] | ((uint32_t)tb16[p][1] << 16); vb.y = tb16[p][2] | ((uint32_t)tb16[p][3] << 16);
-          vb.z = tb16[p][4] | ((uint32_t)tb16[p][5] << 16); vb.w = tb16[p][6] | ((uint32_t)tb16[p][7] << 16);
-          v0.x = t0[p][0] | ((uint32_t)t0[p][1] << 16); v0.y = t0[p][2] | ((uint32_t)t0[p][3] << 16);
-          v0.z = t0[p][4] | ((uint32_t)t0[p][5] << 16); v0.w = t0[p][6] | ((uint32_t)t0[p][7] << 16);
-          v1.x = t1[p][0] | ((uint32_t)t1[p][1] << 16); v1.y = t1[p][2] | ((uint32_t)t1[p][3] << 16);
-          v1.z = t1[p][4] | ((uint32_t)t1[p][5] << 16); v1.w = t1[p][6] | ((uint32_t)t1[p][7] << 16);
-          // tile order in a stage: B planes, then channel 0 A planes, then channel 1 A planes
-          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = vb;
-          *(uint4 *)(st + (size_t)(np + p) * TILE_BYTES + off) = v0;
-          *(uint4 *)(st + (size_t)(2 * np + p) * TILE_BYTES + off) = v1;
+          uint4 v;
+          v.x = tbv[p][0] | ((uint32_t)tbv[p][1] << 16); v.y = tbv[p][2] | ((uint32_t)tbv[p][3] << 16);
+          v.z = tbv[p][4] | ((uint32_t)tbv[p][5] << 16); v.w = tbv[p][6] | ((uint32_t)tbv[p][7] << 16);
+          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = v;  // B planes first
+          for (int lc = 0; lc < nch; lc++) {
+            const uint16_t *t = tav[lc][p];
+            v.x = t[0] | ((uint32_t)t[1] << 16); v.y = t[2] | ((uint32_t)t[3] << 16);
+            v.z = t[4] | ((uint32_t)t[5] << 16); v.w = t[6] | ((uint32_t)t[7] << 16);
+            *(uint4 *)(st + (size_t)(np * (1 + lc) + p) * TILE_BYTES + off) = v;  // then A planes per channel
+          }
         }
       }
       fence_proxy_async();
@@ -253,20 +280,27 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
     }
   } else if (warp < 8) {
     // ---------------- epilogue: drain FP32 sub-chunk sums into FP64 ----------------
-    const int q = warp - 4;                 // TMEM lanes 32q..32q+31
+    const int q = warp - 4;                 // this warp may read TMEM lanes 32q..32q+31
     const int row = ta * BM + 32 * q + lane;
+    const int nacc = a.exact ? 2 : 1;
     for (int sc = 0; sc < nsub; sc++) {
       const int b = sc & 1, use = sc >> 1;
       if (!mbar_wait(&accfull[b], use & 1, abort_flag)) break;
       tc_fence_after();
-      for (int ch = 0; ch < 2; ch++) {
-        const double inv = 1.0 / ((double)sB * (double)(ch == 0 ? sA0 : sA1));
-        double *dst = a.M64 + (((size_t)e * 2 + ch) * a.Mp + row) * a.Mp + tb * BN;
+      for (int lc = 0; lc < nch; lc++) {
+        const double ia = 1.0 / (double)a.sA[(size_t)(cbase + lc) * a.Mp + row];
+        double *dst = a.M64 + (((size_t)e * 2 + ch0 + lc) * a.Mp + row) * a.Mp + tb * BN;
+        const float *sbc = a.sB + tb * BN;
         for (int c0 = 0; c0 < BN; c0 += 32) {
-          float v[32];
-          tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((b * 2 + ch) * BN + c0), v);
+          float v[32], w[32];
+          const uint32_t col = (uint32_t)(((b * nch + lc) * nacc) * BN + c0);
+          tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
+          if (nacc == 2) tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col + BN, w);
 #pragma unroll 4
-          for (int j = 0; j < 32; j++) dst[c0 + j] += (double)v[j] * inv;
+          for (int j = 0; j < 32; j++) {
+            const double s = nacc == 2 ? (double)v[j] + (double)w[j] : (double)v[j];
+            dst[c0 + j] += s * ia / (double)sbc[c0 + j];
+          }
         }
       }
       tc_fence_before();
@@ -280,36 +314,45 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       const int b = sc & 1, buse = sc >> 1;
       if (buse > 0 && !mbar_wait(&accempty[b], (buse - 1) & 1, abort_flag)) break;
       tc_fence_after();
-      const int kend = min(nkb, (sc + 1) * a.ksub_blocks);
-      bool first = true;
-      for (; kb < kend; kb++) {
+      const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
+      bool ok = true;
+      for (kb = kbeg; kb < kend; kb++) {
         const int s = kb & 1, use = kb >> 1;
-        if (!mbar_wait(&full[s], use & 1, abort_flag)) break;
+        if (!mbar_wait(&full[s], use & 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
         const uint32_t st = smem_u32(stage_base + (size_t)s * tiles_per_stage * TILE_BYTES);
-        for (int kk = 0; kk < BK / 16; kk++) {
-          for (int ch = 0; ch < 2; ch++) {
-            const uint32_t d = tmem + (uint32_t)((b * 2 + ch) * BN);
-            // products with plane(A) + plane(B) <= np - 1
+        const int nacc = a.exact ? 2 : 1;
+        for (int kk = 0; kk < BK / 16; kk++)
+          for (int lc = 0; lc < nch; lc++) {
+            const uint32_t d0 = tmem + (uint32_t)(((b * nch + lc) * nacc) * BN);
+            const bool fresh = (kb == kbeg && kk == 0);
+            int idx0 = 0, idx1 = 0;
+            // products of planes pa (A) and pb (B) with pa + pb <= np - 1; with the
+            // exact scheme the leading product has its own accumulator
             for (int pa = 0; pa < np; pa++)
               for (int pb = 0; pa + pb < np; pb++) {
-                const uint64_t ad = make_desc(st + (uint32_t)((np * (1 + ch) + pa) * TILE_BYTES) + kk * 32);
+                const uint64_t ad = make_desc(st + (uint32_t)((np * (1 + lc) + pa) * TILE_BYTES) + kk * 32);
                 const uint64_t bd = make_desc(st + (uint32_t)(pb * TILE_BYTES) + kk * 32);
-                mma_f16(d, ad, bd, idesc, first ? 0 : 1);
-                first = false;
+                const bool lead = nacc == 2 && pa == 0 && pb == 0;
+                if (lead || nacc == 1) {
+                  mma_f16(d0, ad, bd, idesc, (fresh && idx0 == 0) ? 0 : 1);
+                  idx0++;
+                } else {
+                  mma_f16(d0 + BN, ad, bd, idesc, (fresh && idx1 == 0) ? 0 : 1);
+                  idx1++;
+                }
               }
-            if (ch == 0) first = (kb == sc * a.ksub_blocks && kk == 0);  // channel 1 starts fresh too
           }
-          first = false;
-        }
         mma_commit(&empty[s]);
       }
+      if (!ok) break;
       mma_commit(&accfull[b]);
     }
     // wait for every MMA this thread issued before tensor memory is released
     mma_commit(fin);
     mbar_wait(fin, 0, abort_flag);
   }
+  __syncwarp();
   if (tid == 0 && *abort_flag) atomicExch(a.err, 4);
   tc_fence_before();
   __syncthreads();
@@ -323,14 +366,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
 // helpers: transpose the batch's pair densities and weights into the GEMM's
 // K-major operands, batch maxima, Gamma rows/columns, final assembly.
 
-// Yt[g][K] = Re rho, Yt[Gp+g][K] = Im rho, K = k*npair + p (rho is [p][k][g])
-__global__ void yt_kernel(const float2 *__restrict__ rho, int npair, int ntk, int ng, int Gp, int Kp,
+// Yt[g][K] = Re rho, Yt[Gp+g][K] = Im rho, K = k*npair + p (rho is [p][k][g],
+// float2 or, with FP64 pair densities, double2 rounded to float as chiqw_sub.F:201)
+template <typename R>
+__global__ void yt_kernel(const R *__restrict__ rho, int npair, int ntk, int ng, int Gp, int Kp,
                           float *__restrict__ Yt, const double2 *__restrict__ head, int g0) {
   const long K = (long)blockIdx.x;  // one K per block
   const int k = (int)(K / npair), p = (int)(K % npair);
-  const float2 *src = rho + ((size_t)p * ntk + k) * ng;
+  const R *src = rho + ((size_t)p * ntk + k) * ng;
   for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-    float2 v = src[g];
+    float2 v = make_float2((float)src[g].x, (float)src[g].y);
     if (head && g == g0) {
       double2 h = head[((size_t)p * ntk + k) * 3];
       v = make_float2((float)h.x, (float)h.y);
@@ -340,14 +385,15 @@ __global__ void yt_kernel(const float2 *__restrict__ rho, int npair, int ntk, in
   }
 }
 
-// wt[e][K] = w[(p*nen + e)*ntk + k]
-__global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int nen, int Kp, float2 *__restrict__ wt) {
+// wt[e][K] = w[(p*nen + e)*ntk + k] as float pairs: hi = float(v), lo = float(v - hi)
+__global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int nen, int Kp, float4 *__restrict__ wt) {
   const long K = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (K >= (long)npair * ntk) return;
   const int k = (int)(K / npair), p = (int)(K % npair);
   for (int e = 0; e < nen; e++) {
     double2 v = w[((size_t)p * nen + e) * ntk + k];
-    wt[(size_t)e * Kp + K] = make_float2((float)v.x, (float)v.y);
+    const float rh = (float)v.x, ih = (float)v.y;
+    wt[(size_t)e * Kp + K] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
   }
 }
 
@@ -355,7 +401,7 @@ __device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
   atomicMax((int *)addr, __float_as_int(v));  // valid for non-negative floats
 }
 
-__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float2 *__restrict__ wt, int nen, int Kp,
+__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float4 *__restrict__ wt, int nen, int Kp,
                              long Kn, float *__restrict__ out) {
   float m = 0.f;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nY; i += (size_t)gridDim.x * blockDim.x)
@@ -365,9 +411,9 @@ __global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const floa
   for (int e = 0; e < nen; e++) {
     float mr = 0.f, mi = 0.f;
     for (long K = (long)blockIdx.x * blockDim.x + threadIdx.x; K < Kn; K += (long)gridDim.x * blockDim.x) {
-      float2 v = wt[(size_t)e * Kp + K];
+      float4 v = wt[(size_t)e * Kp + K];
       mr = fmaxf(mr, fabsf(v.x));
-      mi = fmaxf(mi, fabsf(v.y));
+      mi = fmaxf(mi, fabsf(v.z));
     }
     for (int o = 16; o; o >>= 1) {
       mr = fmaxf(mr, __shfl_xor_sync(0xffffffffu, mr, o));
@@ -375,6 +421,30 @@ __global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const floa
     }
     if ((threadIdx.x & 31) == 0) { atomic_max_pos(&out[1 + 2 * e], mr); atomic_max_pos(&out[2 + 2 * e], mi); }
   }
+}
+
+// per-row maxima of Yt over the batch's K
+__global__ void rowmax_kernel(const float *__restrict__ Yt, int Kp, long Kn, float *__restrict__ rowmax) {
+  const float *r = Yt + (size_t)blockIdx.x * Kp;
+  float m = 0.f;
+  for (long K = threadIdx.x; K < Kn; K += blockDim.x) m = fmaxf(m, fabsf(r[K]));
+  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ float sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, sm[i]);
+    rowmax[blockIdx.x] = fmaxf(m, sm[0]);
+  }
+}
+
+// row scales: B rows from the row maximum, A rows from row maximum x channel maximum
+__global__ void scales_kernel(const float *__restrict__ rowmax, const float *__restrict__ maxes, int Mp, int nen,
+                              int top, float *__restrict__ sB, float *__restrict__ sA) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= Mp) return;
+  sB[a] = scale_for(rowmax[a], top);
+  for (int c = 0; c < 2 * nen; c++) sA[(size_t)c * Mp + a] = scale_for(rowmax[a] * maxes[1 + c], top);
 }
 
 // Gamma, directions 2 and 3: G=0 row and column in FP64 from the FP32 densities
@@ -465,9 +535,9 @@ void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st) {
   RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
 }
 
-int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *w, const double2 *head, int npair, int ntk,
-                      int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol, int *err,
-                      cudaStream_t st) {
+int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const double2 *w, const double2 *head,
+                      int npair, int ntk, int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol,
+                      int *err, cudaStream_t st) {
   (void)chi;
   if (npair == 0) return 0;
   int launches = 0;
@@ -475,20 +545,27 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *w, cons
   const long Kn = (long)npair * ntk;
   const int Kp = (int)(((Kn + BK - 1) / BK) * BK);
   // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float2, maxes
-  const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float2) * (size_t)nen * Kp;
+  const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float4) * (size_t)nen * Kp;
   const size_t mxbytes = sizeof(float) * (1 + 2 * (size_t)nen);
-  unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, ybytes + wbytes + mxbytes + 256);
+  const size_t sbytes = sizeof(float) * (size_t)Mp * (2 + 2 * (size_t)nen);  // rowmax, sB, sA
+  unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, ybytes + wbytes + mxbytes + sbytes + 512);
   float *Yt = (float *)base;
-  float2 *wt = (float2 *)(base + ybytes);
+  float4 *wt = (float4 *)(base + ybytes);
   float *maxes = (float *)(base + ybytes + wbytes);
+  float *rowmax = (float *)(base + ybytes + wbytes + ((mxbytes + 255) / 256) * 256);
+  float *sBv = rowmax + Mp, *sAv = sBv + Mp;
   RP_CUDA(cudaMemsetAsync(base, 0, ybytes + wbytes + mxbytes, st));
   if (Kn > 0x7fffffffL) fail(1, "batch too large");
-  yt_kernel<<<(unsigned)Kn, 128, 0, st>>>(rho, npair, ntk, ng, Gp, Kp, Yt, head, g0);
+  if (rho64) yt_kernel<double2><<<(unsigned)Kn, 128, 0, st>>>(rho64, npair, ntk, ng, Gp, Kp, Yt, head, g0);
+  else yt_kernel<float2><<<(unsigned)Kn, 128, 0, st>>>(rho, npair, ntk, ng, Gp, Kp, Yt, head, g0);
   wt_kernel<<<(unsigned)((Kn + 255) / 256), 256, 0, st>>>(w, npair, ntk, nen, Kp, wt);
   maxes_kernel<<<1024, 256, 0, st>>>(Yt, (size_t)Mp * Kp, wt, nen, Kp, Kn, maxes);
-  launches += 3;
+  rowmax_kernel<<<Mp, 256, 0, st>>>(Yt, Kp, Kn, rowmax);
+  const int exact = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 1 : 0;
+  scales_kernel<<<(Mp + 127) / 128, 128, 0, st>>>(rowmax, maxes, Mp, nen, exact ? 7 : 14, sBv, sAv);
+  launches += 5;
   RP_CUDA(cudaGetLastError());
-  if (head && rowcol) {
+  if (head && rowcol && !rho64) {
     dim3 g(ng, nen, 2);
     gamma_rowcol_f32_kernel<<<g, 256, 0, st>>>(rho, w, head, npair, ntk, ng, nen, g0, rowcol);
     launches++;
@@ -506,15 +583,23 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *w, cons
   TcArgs a;
   a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.M64 = (double *)ws.part; a.err = err;
   a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;
-  a.nplanes = precision == RP_PREC_BF16X3 ? 3 : 2;
+  a.nplanes = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2;
   a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
-  a.ksub_blocks = 16;  // 1024 K per FP32 sub-chunk
+  a.exact = exact;
+  a.sB = sBv; a.sA = sAv;
+  // two accumulators per channel in the exact scheme: one channel per CTA keeps
+  // double-buffered accumulators within the 512 TMEM columns
+  a.nch = (a.nplanes == 2 && !exact) ? 2 : 1;
+  // default 512 K per FP32 sub-chunk: the correction accumulator's rounding
+  // bias grows with its length; integer partial sums must stay below 2^24
+  a.ksub_blocks = ws.ksub > 0 ? ws.ksub : 8;
+  if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
-  const int tiles_per_stage = 3 * a.nplanes;
+  const int tiles_per_stage = a.nplanes * (1 + a.nch);
   const size_t smem = 1024 + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES + 128;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
   RP_CUDA(cudaFuncSetAttribute(tc_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)tl.size(), nen);
+  dim3 grid((unsigned)tl.size(), nen * (2 / a.nch));
   tc_gram_kernel<<<grid, NTHREADS, smem, st>>>(a);
   launches++;
   RP_CUDA(cudaGetLastError());

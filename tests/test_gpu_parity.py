@@ -98,3 +98,33 @@ def test_bad_input_reports_error(case_dir, fresh_copy):
             ctx.chi0_q(99)
     with pytest.raises(RuntimeError, match="cannot open"):
         rp.Context(root + "/nonexistent", rp.default_params(), EM_TEST)
+
+
+@pytest.mark.parametrize("case,qs", [("tiny", [1, 2, 5]), ("tiny_metal", [1, 3]), ("config1", [1, 2, 7])])
+@pytest.mark.parametrize("pair64", [0, 1])
+@pytest.mark.parametrize("prec", [rp.PREC_FP16X3, rp.PREC_BF16X3, rp.PREC_FP16X2])
+def test_chi0_tensor_core_matches_oracle(case_dir, fresh_copy, case, qs, prec, pair64):
+    """Split-precision tcgen05 contraction: chi0 and eps^-1 within 1e-6 (normwise
+    per frequency) of the FP64 oracle for the three-term FP16 split, with FP32
+    or FP64 pair densities."""
+    if pair64 and prec != rp.PREC_FP16X3:
+        pytest.skip("FP64 pair densities are checked with one split")
+    kw = run_params(case)
+    ref_root = fresh_copy(case_dir(case_name(case)))
+    _oracle_run(ref_root, kw, qidx=qs)
+    with rp.Context(ref_root, rp.default_params(precision=prec, pair_fp64=pair64, **kw), EM_TEST) as ctx:
+        worst = worst_eps = 0.0
+        for iq in qs:
+            chi = ctx.chi0_q(iq)
+            ref = orc.read_chi_dump(os.path.join(ref_root, "dir-eps", "q%03d" % iq, "dat.chi0"))
+            worst = max(worst, normwise_err(chi, ref))
+            eps = ctx.epsinv_q()
+            ng, nen = eps.shape[0], eps.shape[2]
+            er = read_eps_record(os.path.join(ref_root, "dir-eps", "q%03d" % iq, "dat.epsqw.600"), ng, nen)
+            worst_eps = max(worst_eps, normwise_err(eps[..., 0], er))
+    print(f"{case} prec={prec} pair64={pair64}: chi rel err {worst:.3e} epsinv {worst_eps:.3e}")
+    # the 1e-6 target holds for the three-term FP16 split; the BF16 split keeps
+    # 23 bits and the two-term FP16 split 22, both held to 1e-5
+    bound = 1e-6 if prec == rp.PREC_FP16X3 else 1e-5
+    assert worst < bound
+    assert worst_eps < bound
