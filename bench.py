@@ -1,0 +1,354 @@
+"""Benchmark: chiqw seconds per q-point (all frequencies) on one GB300.
+
+Workload ``chiqw_8x8x8k_200b`` (seeded synthetic, no dataset): fcc cell
+a = 15.84 bohr, 8x8x8 Gamma-centred k mesh (512 q), 200 bands (8 occupied,
+1536 band pairs), 20 Ry wave-function cutoff (~1514 plane waves), FFT box 36^3,
+dielectric cutoff 11 Ry (~600 G), 20 frequencies (10 real 0-30 eV, 10
+imaginary on a Gauss-Legendre grid over 0-30 eV), band-cRPA window 9-11.
+
+A step is one q point: rp_chi0_q (tetrahedron weights, pair densities,
+contraction) + rp_epsinv_q (eps build and FP64 inversion).  `value` is the
+device time per q point of the split-precision (FP16x3) path with every input
+resident in HBM; `e2e` is the same through the C ABI with host output
+buffers (chi and eps^-1 copied back every step).  Inputs (38 GB of real-space
+wave functions, 3.8 GB of pair densities per q) are larger than L2, so no
+flush is needed.  The plain FP64 GPU path and its chi error are measured on a
+1/16 band-pair sample of one q and scaled linearly in the pair count (every
+stage but the eps inversion is linear in it).  The CPU baseline is the C
+restatement (oracle) on the host cores on a bounded pair sample, scaled the
+same way.
+
+--impl reference runs that CPU restatement as the reference arm: the
+reference (Fortran + MPI + MKL) cannot be built here (no Fortran compiler).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+AU = 27.21151
+WORKLOAD = "chiqw_8x8x8k_200b"
+
+
+def make_spec(case="full"):
+    from respackdev_gb300 import synth
+    if case == "small":
+        # the same cell, cutoffs, FFT box and frequencies on a 4x4x4 mesh with 100
+        # bands: the kernels of the full workload at a size an ncu capture can hold
+        return synth.SynthSpec(lattice="fcc", a=15.84, nk=(4, 4, 4), nbands=100, nocc=8, ecut_psi=20.0,
+                               seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False)
+    return synth.SynthSpec(lattice="fcc", a=15.84, nk=(8, 8, 8), nbands=200, nocc=8, ecut_psi=20.0,
+                           seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False)
+
+
+def frequencies():
+    re = np.linspace(0.0, 30.0, 10)
+    x, _ = np.polynomial.legendre.leggauss(10)
+    im = 15.0 * (x + 1.0)
+    return np.concatenate([re, 1j * im]) / AU
+
+
+RUN_PARAMS = dict(ecut_for_eps=11.0, green_func_delt=0.2721, flg_crpa=1)
+FFT_BOX = (36, 36, 36)
+
+
+def prepare(root, case="full"):
+    from respackdev_gb300 import synth
+    t = time.time()
+    synth.make_case(root, make_spec(case))
+    return time.time() - t
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("bf16_tflops_sustained"), d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
+    return 1700.0, 1900.0, 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per tensor-core contraction launch from the committed ncu summary, if any."""
+    p = os.path.join(HERE, "profiles", "tc_gram_kernel_chiqw.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch_scaled:"):
+            try:
+                return float(line.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(root, nthreads, npair_sample, em, iq=2):
+    """The C restatement on host cores: one q, the first npair_sample pairs,
+    scaled to the full pair count."""
+    from oracle import oracle as orc
+    orc.build()
+    shutil.rmtree(os.path.join(root, "dir-eps"), ignore_errors=True)
+    p = orc.make_params(em=em, nthreads=nthreads, max_pairs=npair_sample, calc_num_k=[iq], fft_box=FFT_BOX,
+                        write_eps=0, **RUN_PARAMS)
+    rep = orc.calc_chiqw(root, p)
+    frac = rep.npair_full_last / max(1, rep.npair_last)
+    return rep.seconds_last_q * frac, rep
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    tmp = tempfile.mkdtemp(prefix="rp_bench_ref_")
+    try:
+        prepare(tmp)
+        em = frequencies()
+        for _ in range(args.warmup):
+            cpu_baseline(tmp, nthreads, nthreads, em)
+        vals = []
+        t0 = time.time()
+        for _ in range(args.steps):
+            v, rep = cpu_baseline(tmp, nthreads, nthreads, em)
+            vals.append(v)
+        wall = time.time() - t0
+        value = float(np.mean(vals))
+        line = {"metric": "chiqw s/q-point (all w)", "value": value, "unit": "s/q-point", "impl": "reference",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "npair": rep.npair_full_last, "ng": rep.ng_last, "ntk": rep.ntk,
+                           "nen": rep.nen, "fft_box": list(rep.fft_box), "parallelism": "openmp-host"},
+                "cpu_baseline": {"value": value, "unit": "s/q-point", "cores": nthreads, "kind": "port",
+                                 "sample": f"one q point, {rep.npair_last} of {rep.npair_full_last} band pairs, "
+                                           f"scaled linearly in the pair count (C restatement of chiqw; the Fortran "
+                                           f"reference cannot be built here)"},
+                "e2e": {"value": value, "unit": "s/q-point", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
+def normwise(a, b):
+    w = 0.0
+    for i in range(b.shape[2]):
+        for j in range(b.shape[3]):
+            d = np.abs(b[:, :, i, j]).max()
+            if d:
+                w = max(w, float(np.abs(a[:, :, i, j] - b[:, :, i, j]).max() / d))
+    return w
+
+
+def run_gpu(args):
+    from respackdev_gb300 import build
+    from respackdev_gb300 import chiqw as rp
+    build.build()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+        dist.init_process_group("gloo")
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    tmp = tempfile.mkdtemp(prefix="rp_bench_")
+    try:
+        t_prep = prepare(tmp, args.case)
+        em = frequencies()
+        params = rp.default_params(precision=rp.PREC_FP16X3, fft_box=FFT_BOX, device=dev, **RUN_PARAMS)
+        t0 = time.time()
+        ctx = rp.Context(tmp, params, em)
+        t_setup = time.time() - t0
+        info = ctx.info()
+        nq_all = ctx.L.rp_num_qirr(ctx._h)
+        # q points of this rank (weak scaling: every rank takes its own q points), Gamma excluded
+        qs = [iq for iq in range(2, nq_all + 1)]
+        mine = qs[rank::world]
+        need = args.warmup + args.steps
+        mine = (mine * (need // max(1, len(mine)) + 1))[:need]
+        for iq in mine[: args.warmup]:
+            ctx.chi0_q(iq, fetch=False)
+            ctx.epsinv_q(fetch=False)
+        # --- device-resident timing ---
+        launches0 = ctx.kernel_launches()
+        if dist:
+            dist.barrier()
+        stage = np.zeros(5)
+        tcg = 0.0
+        with ClockSampler(dev) as clk:
+            t0 = time.perf_counter()
+            for iq in mine[args.warmup:]:
+                ctx.chi0_q(iq, fetch=False)
+                st1 = ctx.stage_times()
+                ctx.epsinv_q(fetch=False)
+                st2 = ctx.stage_times()
+                stage += np.array([st1[0], st1[1], st1[2], st2[3], st1[4]])
+                tcg += ctx.tc_gram_seconds()
+            elapsed = time.perf_counter() - t0
+        launches = ctx.kernel_launches() - launches0
+        if dist:
+            import torch
+            t = torch.tensor([elapsed], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            elapsed = float(t.item())
+        value = elapsed / (args.steps * world)
+        # --- end to end through the C ABI with host buffers ---
+        ng, nen = ctx.ng, info.nen
+        e2e_steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for iq in mine[args.warmup: args.warmup + e2e_steps]:
+            ctx.chi0_q(iq, fetch=True)
+            ctx.epsinv_q(fetch=True)
+        e2e = (time.perf_counter() - t0) / e2e_steps
+        d2h = 2 * ng * ng * nen * 16
+        h2d = ng * 3 * 4 + info.ntk * 4 * 4 + 2 * 1536 * 4
+        # --- plain FP64 path and the error of the fast path on a pair sample of one q ---
+        npair_full = info.n_occ * info.n_vir
+        iq0 = mine[args.warmup]
+        plain = err = None
+        sample_pairs = 96
+        if not args.no_plain:
+            pf = rp.default_params(precision=rp.PREC_FP64, fft_box=FFT_BOX, device=dev, max_pairs=sample_pairs,
+                                   **RUN_PARAMS)
+            with rp.Context(tmp, pf, em) as c64:
+                chi64 = c64.chi0_q(iq0)
+                s64 = c64.stage_times()
+                c64.epsinv_q(fetch=False)
+                e64 = c64.stage_times()[3]
+            ps = rp.default_params(precision=rp.PREC_FP16X3, fft_box=FFT_BOX, device=dev, max_pairs=sample_pairs,
+                                   **RUN_PARAMS)
+            with rp.Context(tmp, ps, em) as cs:
+                chis = cs.chi0_q(iq0)
+            err = normwise(chis, chi64)
+            plain = s64[4] * npair_full / sample_pairs + e64
+        # --- roofline of the tensor-core contraction ---
+        tflops_sus, tflops_burst, hbm, src = measured_peaks()
+        K = npair_full * info.ntk
+        alg_flops_per_q = 8.0 * ng * ng * K * nen
+        achieved = alg_flops_per_q * args.steps / tcg / 1e12 if tcg > 0 else None
+        roof = {"bound": "tensor", "kernel": "tc_gram_kernel", "achieved": achieved, "peak": tflops_sus,
+                "unit": "TFLOP/s", "frac": (achieved / tflops_sus) if achieved else None,
+                "peak_source": f"{src} bf16 sustained", "traffic": profile_traffic(),
+                "tensor_products_per_real_product": 6,
+                "achieved_tensor_tflops": achieved * 6 if achieved else None,
+                "algorithmic_flops_per_q": alg_flops_per_q}
+        # --- CPU baseline (rank 0, host cores, bounded sample) ---
+        cpu = None
+        if rank == 0 and not args.no_cpu and args.case == "full":
+            nthr = os.cpu_count() or 1
+            v, rep = cpu_baseline(tmp, nthr, nthr, em, iq=iq0)
+            cpu = {"value": v, "unit": "s/q-point", "cores": nthr, "kind": "port",
+                   "sample": f"one q point, {rep.npair_last} of {rep.npair_full_last} band pairs on {nthr} threads, "
+                             f"scaled linearly in the pair count"}
+        clocks = clk.summary()
+        if rank == 0:
+            line = {"metric": "chiqw s/q-point (all w) vs plain FP64 GPU at chi rel err<=1e-6; % roofline",
+                    "value": value, "unit": "s/q-point", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                    "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": False, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "fp16x3-split tensor contraction, f32 pair densities, f64 weights/eps",
+                    "data": "synthetic (seeded generator, dir-wfn files)",
+                    "config": {"workload": WORKLOAD if args.case == "full" else WORKLOAD + "_small", "ntk": info.ntk, "nbands": info.ncb, "npair": npair_full,
+                               "npw_max": info.ntg, "ng": ng, "nen": nen, "fft_box": list(info.fft_box),
+                               "l2": "inputs larger than L2 (38 GB wave functions, 3.8 GB pair densities per q)",
+                               "parallelism": f"q-shard x{world}"},
+                    "plain_fp64_s_per_q": plain, "speedup_vs_plain_fp64": (plain / value) if plain else None,
+                    "plain_fp64_sample": f"{sample_pairs} of {npair_full} pairs on q {iq0}, scaled linearly",
+                    "chi_rel_err_vs_fp64": err,
+                    "stage_seconds_per_q": {"tetra": stage[0] / args.steps, "pair_density": stage[1] / args.steps,
+                                            "contraction": stage[2] / args.steps, "eps_inverse": stage[3] / args.steps},
+                    "setup_seconds": t_setup, "input_generation_seconds": t_prep,
+                    "roofline": roof, "clocks": clocks,
+                    "e2e": {"value": e2e, "unit": "s/q-point", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                            "note": "wave functions uploaded once per run (setup_seconds)"},
+                    "gpu_launches": launches, "cpu_baseline": cpu}
+            print(json.dumps(line), flush=True)
+        ctx.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+        if dist:
+            dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: 4x4x4 k, 100 bands, same kernels (for profiler captures)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

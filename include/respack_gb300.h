@@ -98,6 +98,10 @@ int rp_ctx_info(const rp_ctx *ctx, rp_info *info);
 /* Number of entries of dat.sample-k (= candidate q points). */
 int rp_num_qirr(const rp_ctx *ctx);
 
+/* Sizes of q point iq without computing it: ng (dielectric G sphere of
+ * make_KG0, chiqw_sub.F:773-812) and ndir (3 at Gamma, else 1). */
+int rp_q_dims(const rp_ctx *ctx, int iq, int *ng, int *ndir);
+
 /* chi0(G,G',w) of irreducible point iq (1-based index of dat.sample-k), after
  * /VOLUME and before the spin factor: the array chiqw of chiqw.F:1476 (q != 0,
  * layout (ng, ng, nen)) or chiqwgm of :1989 (Gamma, (ng, ng, nen, 3)).
@@ -123,8 +127,9 @@ int rp_calc_chiqw(const char *root, const char *namelist_text);
 
 /* Seconds spent in each stage of the last rp_chi0_q + rp_epsinv_q (device
  * time from CUDA events): [0] tetrahedron weights, [1] pair densities,
- * [2] contraction, [3] eps build + inversion, [4] total chi0_q. */
-int rp_stage_times(const rp_ctx *ctx, double *t5);
+ * [2] contraction, [3] eps build + inversion, [4] total chi0_q, [5] the
+ * tensor-core Gram kernel alone (0 on the FP64 path). */
+int rp_stage_times(const rp_ctx *ctx, double *t6);
 
 /* Number of kernel launches issued by this context so far. */
 long long rp_kernel_launches(const rp_ctx *ctx);

@@ -29,7 +29,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 # files whose arithmetic should round like the CPU reference (no FMA contraction)
-NOFMAD = {"rp_tetra.cu"}
+NOFMAD: set = set()
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", f"-I{CUDA_HOME}/include"]
 
 

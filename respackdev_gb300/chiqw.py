@@ -76,6 +76,8 @@ def load() -> C.CDLL:
     L.rp_calc_chiqw.argtypes = [C.c_char_p, C.c_char_p]
     L.rp_calc_chiqw.restype = C.c_int
     L.rp_stage_times.argtypes = [vp, dp]
+    L.rp_q_dims.argtypes = [vp, C.c_int, ip, ip]
+    L.rp_q_dims.restype = C.c_int
     L.rp_kernel_launches.argtypes = [vp]
     L.rp_kernel_launches.restype = C.c_longlong
     L.rp_last_error.argtypes = [vp]
@@ -143,17 +145,23 @@ class Context:
         self.L.rp_ctx_info(self._h, C.byref(inf))
         return inf
 
+    def q_dims(self, iq: int):
+        ng, nd = C.c_int(0), C.c_int(0)
+        self._check(self.L.rp_q_dims(self._h, iq, C.byref(ng), C.byref(nd)), "rp_q_dims")
+        return ng.value, nd.value
+
     def chi0_q(self, iq: int, fetch: bool = True) -> Optional[np.ndarray]:
         """chi0 (after /VOLUME, before the spin factor) as (ng, ng, nen, ndir), column-major G order."""
-        ng, nd = C.c_int(0), C.c_int(0)
-        self._check(self.L.rp_chi0_q(self._h, iq, None, C.byref(ng), C.byref(nd)), "rp_chi0_q")
-        self.ng, self.ndir = ng.value, nd.value
+        ng, nd = self.q_dims(iq)
+        nen = self.info().nen
+        out = np.empty(nd * nen * ng * ng, dtype=np.complex128) if fetch else None
+        ngo, ndo = C.c_int(0), C.c_int(0)
+        self._check(self.L.rp_chi0_q(self._h, iq, out.ctypes.data if fetch else None, C.byref(ngo), C.byref(ndo)),
+                    "rp_chi0_q")
+        self.ng, self.ndir = ngo.value, ndo.value
         if not fetch:
             return None
-        nen = self.info().nen
-        out = np.empty(self.ndir * nen * self.ng * self.ng, dtype=np.complex128)
-        self._check(self.L.rp_chi0_q(self._h, iq, out.ctypes.data, None, None), "rp_chi0_q")
-        return out.reshape(self.ndir, nen, self.ng, self.ng).transpose(3, 2, 1, 0)
+        return out.reshape(nd, nen, ng, ng).transpose(3, 2, 1, 0)
 
     def epsinv_q(self, fetch: bool = True) -> Optional[np.ndarray]:
         nen = self.info().nen
@@ -168,9 +176,13 @@ class Context:
         self._check(self.L.rp_write_q(self._h, (root or self.root).encode()), "rp_write_q")
 
     def stage_times(self) -> np.ndarray:
-        t = (C.c_double * 5)()
+        t = (C.c_double * 6)()
         self.L.rp_stage_times(self._h, t)
         return np.array(t[:])
+
+    def tc_gram_seconds(self) -> float:
+        """Device time of the tensor-core Gram kernel in the last chi0_q."""
+        return float(self.stage_times()[5])
 
     def kernel_launches(self) -> int:
         return int(self.L.rp_kernel_launches(self._h))

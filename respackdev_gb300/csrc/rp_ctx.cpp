@@ -71,7 +71,7 @@ struct rp_ctx {
   bool have_chi = false, have_eps = false;
   std::vector<cd> h_chi, h_eps;
   cudaEvent_t ev[6]{};
-  double times[5]{};
+  double times[6]{};
   ~rp_ctx() {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
@@ -351,6 +351,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   float tot = 0;
   RP_CUDA(cudaEventElapsedTime(&tot, c->ev[5], c->ev[4]));
   c->times[0] = tms[0] * 1e-3; c->times[1] = tms[1] * 1e-3; c->times[2] = tms[2] * 1e-3; c->times[4] = tot * 1e-3;
+  c->times[5] = fast ? c->tcw.gram_seconds : 0.0;
   c->have_chi = true;
 }
 
@@ -363,7 +364,7 @@ static void epsinv_run(rp_ctx *c) {
   c->A.ensure(sizeof(cd) * sz);
   c->eps.ensure(sizeof(cd) * sz);
   c->prow.ensure(sizeof(cd) * (size_t)nmat * ng);
-  c->fcol.ensure(sizeof(cd) * (size_t)nmat * ng);
+  c->fcol.ensure(sizeof(cd) * ((size_t)nmat * ng + nmat));  // pivot column copies + pivot reciprocals
   c->piv.ensure(sizeof(int) * (size_t)nmat * ng);
   c->used.ensure(sizeof(int) * (size_t)nmat * ng);
   rp::EpsArgs a;
@@ -507,10 +508,19 @@ int rp_write_q(rp_ctx *c, const char *root) {
   return guarded(c, [&] { write_q(c, root ? root : c->root); });
 }
 
-int rp_stage_times(const rp_ctx *c, double *t5) {
-  if (!c || !t5) return 1;
-  for (int i = 0; i < 5; i++) t5[i] = c->times[i];
+int rp_stage_times(const rp_ctx *c, double *t6) {
+  if (!c || !t6) return 1;
+  for (int i = 0; i < 6; i++) t6[i] = c->times[i];
   return 0;
+}
+
+int rp_q_dims(const rp_ctx *c, int iq, int *ng, int *ndir) {
+  if (!c) return 1;
+  return guarded(const_cast<rp_ctx *>(c), [&] {
+    rp::QTask t = rp::make_qtask(c->S, iq - 1, 1);
+    if (ng) *ng = t.ng;
+    if (ndir) *ndir = t.gamma ? 3 : 1;
+  });
 }
 
 long long rp_kernel_launches(const rp_ctx *c) { return c ? c->launches : 0; }

@@ -60,9 +60,19 @@ __global__ void eps_build_kernel(const double2 *__restrict__ chi, EpsArgs a, dou
   }
 }
 
+__device__ __forceinline__ double2 crecip(double2 b) {
+  // 1/b by Smith's algorithm
+  if (fabs(b.x) >= fabs(b.y)) {
+    double t = b.y / b.x, d = b.x + b.y * t;
+    return make_double2(1.0 / d, -t / d);
+  }
+  double t = b.x / b.y, d = b.x * t + b.y;
+  return make_double2(t / d, -1.0 / d);
+}
+
 __global__ void gj_select_kernel(double2 *__restrict__ A, int n, int k, double2 *__restrict__ prow,
                                  double2 *__restrict__ fcol, int *__restrict__ piv, int *__restrict__ used,
-                                 int *__restrict__ err) {
+                                 double2 *__restrict__ dinv, int *__restrict__ err) {
   const int m = blockIdx.x;
   const size_t nn = (size_t)n * n;
   double2 *Am = A + m * nn;
@@ -94,6 +104,8 @@ __global__ void gj_select_kernel(double2 *__restrict__ A, int n, int k, double2 
     if (!(sv[0] > 0.0) || si[0] != p) atomicExch(err, 3);
     piv[(size_t)m * n + k] = p;
     um[p] = 1;
+    const double2 pk = Am[p + (size_t)n * k];
+    dinv[m] = (pk.x == 0.0 && pk.y == 0.0) ? make_double2(0.0, 0.0) : crecip(pk);
   }
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     prow[(size_t)m * n + j] = Am[p + (size_t)n * j];
@@ -101,34 +113,25 @@ __global__ void gj_select_kernel(double2 *__restrict__ A, int n, int k, double2 
   }
 }
 
-__device__ __forceinline__ double2 crecip(double2 b) {
-  // 1/b by Smith's algorithm
-  if (fabs(b.x) >= fabs(b.y)) {
-    double t = b.y / b.x, d = b.x + b.y * t;
-    return make_double2(1.0 / d, -t / d);
-  }
-  double t = b.x / b.y, d = b.x * t + b.y;
-  return make_double2(t / d, -1.0 / d);
-}
-
-__global__ void gj_update_kernel(double2 *__restrict__ A, int n, int k, const double2 *__restrict__ prow,
-                                 const double2 *__restrict__ fcol, const int *__restrict__ piv) {
-  const int m = blockIdx.y;
-  const size_t nn = (size_t)n * n;
+// one pivot step on all matrices: block (32 rows x 8 columns) of matrix blockIdx.z
+__global__ void __launch_bounds__(256) gj_update_kernel(double2 *__restrict__ A, int n, int k,
+                                                        const double2 *__restrict__ prow,
+                                                        const double2 *__restrict__ fcol, const int *__restrict__ piv,
+                                                        const double2 *__restrict__ dinv) {
+  const int m = blockIdx.z;
+  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
+  if (i >= n || j >= n) return;
   const int p = piv[(size_t)m * n + k];
-  const double2 pk = prow[(size_t)m * n + k];
-  if (pk.x == 0.0 && pk.y == 0.0) return;  // singular: flagged by the select kernel
-  const double2 d = crecip(pk);
-  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < nn; idx += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(idx % n), j = (int)(idx / n);
-    double2 *a = A + m * nn + idx;
-    if (i == p) {
-      *a = (j == k) ? d : cmul(prow[(size_t)m * n + j], d);
-    } else {
-      const double2 f = cmul(fcol[(size_t)m * n + i], d);
-      if (j == k) *a = make_double2(-f.x, -f.y);
-      else *a = csub(*a, cmul(f, prow[(size_t)m * n + j]));
-    }
+  const double2 d = dinv[m];
+  if (d.x == 0.0 && d.y == 0.0) return;  // singular: flagged by the select kernel
+  double2 *a = A + (size_t)m * n * n + i + (size_t)n * j;
+  const double2 pj = prow[(size_t)m * n + j];
+  if (i == p) {
+    *a = (j == k) ? d : cmul(pj, d);
+  } else {
+    const double2 f = cmul(fcol[(size_t)m * n + i], d);
+    if (j == k) *a = make_double2(-f.x, -f.y);
+    else *a = csub(*a, cmul(f, pj));
   }
 }
 
@@ -164,10 +167,13 @@ int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prow, double2 *fco
   int launches = 0;
   RP_CUDA(cudaMemsetAsync(used, 0, sizeof(int) * (size_t)n * nmat, st));
   const size_t nn = (size_t)n * n;
+  // reciprocals of the pivots live after the pivot column copies
+  double2 *dinv = fcol + (size_t)nmat * n;
+  dim3 ublk(32, 8), ugrid2((n + 31) / 32, (n + 7) / 8, nmat);
   dim3 ugrid((unsigned)std::min<size_t>((nn + 255) / 256, 2048), nmat);
   for (int k = 0; k < n; k++) {
-    gj_select_kernel<<<nmat, 256, 0, st>>>(A, n, k, prow, fcol, piv, used, err);
-    gj_update_kernel<<<ugrid, 256, 0, st>>>(A, n, k, prow, fcol, piv);
+    gj_select_kernel<<<nmat, 256, 0, st>>>(A, n, k, prow, fcol, piv, used, dinv, err);
+    gj_update_kernel<<<ugrid2, ublk, 0, st>>>(A, n, k, prow, fcol, piv, dinv);
     launches += 2;
   }
   RP_CUDA(cudaGetLastError());

@@ -51,7 +51,8 @@ constexpr int BN = 128;          // tile columns (b)
 constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
 constexpr int NSTAGE = 2;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
-constexpr int NPROD = 128, NEPI = 128;
+constexpr int NPROD = 256, NEPI = 128;    // 8 producer warps, 4 epilogue warps, 1 MMA warp
+constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 32;
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
@@ -144,6 +145,29 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
   for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+          taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // power-of-two scale that maps |v| <= vmax below 2^top (m 2^e -> m 2^top)
 __device__ __forceinline__ float scale_for(float vmax, int top) {
   if (!(vmax > 0.f)) return 1.f;
@@ -152,52 +176,43 @@ __device__ __forceinline__ float scale_for(float vmax, int top) {
   return ldexpf(1.f, top - e);
 }
 
-// split the float pair v + vl into nplanes 16-bit terms (fp16 or bf16), raw bits;
-// exact: the leading term is rint(v), an integer the 16-bit format holds exactly
-__device__ __forceinline__ void split16(float v, float vl, int nplanes, int bf16, int exact, uint16_t *t) {
-  float r = v;
-  for (int p = 0; p < nplanes; p++) {
-    if (p == 1) r = r + vl;  // the low word joins once the leading term is removed
-    if (p == 0 && exact) {
-      const float h = rintf(r);
-      t[0] = bf16 ? __bfloat16_as_ushort(__float2bfloat16_rn(h)) : __half_as_ushort(__float2half_rn(h));
-      r = r - h;
-      continue;
-    }
-    if (bf16) {
-      __nv_bfloat16 h = __float2bfloat16_rn(r);
-      t[p] = __bfloat16_as_ushort(h);
-      r = r - __bfloat162float(h);
-    } else {
-      __half h = __float2half_rn(r);
-      t[p] = __half_as_ushort(h);
-      r = r - __half2float(h);
-    }
-  }
-}
-
 // byte offset of element (row, k) of a 128 x 64 16-bit tile in the 128B-swizzled K-major layout
 __device__ __forceinline__ uint32_t swz(int row, int chunk16) {
   return (uint32_t)(row * 128 + ((chunk16 ^ (row & 7)) << 4));
 }
 
+template <int NP, bool EXACT, bool BF16>
+__device__ __forceinline__ void split_t(float v, float vl, uint16_t (&t)[NP]) {
+  float r = v;
+#pragma unroll
+  for (int p = 0; p < NP; p++) {
+    if (p == 1) r = r + vl;  // the low word joins once the leading term is removed
+    float h;
+    if (p == 0 && EXACT) h = rintf(r);
+    else h = BF16 ? __bfloat162float(__float2bfloat16_rn(r)) : __half2float(__float2half_rn(r));
+    t[p] = BF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(h)) : __half_as_ushort(__float2half_rn(h));
+    r = r - h;
+  }
+}
+
+// NP operand planes, NCH channels per CTA, EXACT integer leading plane, BF16 or FP16
+template <int NP, int NCH, bool EXACT, bool BF16>
 __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1024-align the operand area
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int np = a.nplanes;                       // 2 (fp16) or 3 (bf16)
-  const int nch = a.nch;                          // 2 or 1
-  const int tiles_per_stage = np * (1 + nch);     // B planes + nch x A planes
+  constexpr int TPS = NP * (1 + NCH);        // tiles per stage: B planes + NCH x A planes
+  constexpr int NACC = EXACT ? 2 : 1;        // accumulators per channel
   unsigned char *stage_base = smem;
-  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES);
+  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * TPS * TILE_BYTES);
   uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accempty = bars + 6, *fin = bars + 8;
   volatile int *abort_flag = (volatile int *)(bars + 9);
   uint32_t *tmem_slot = (uint32_t *)(bars + 10);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // frequency e and the first channel handled here (channel 0 = Re weight, 1 = Im weight)
-  const int e = nch == 2 ? blockIdx.y : blockIdx.y >> 1;
-  const int ch0 = nch == 2 ? 0 : (blockIdx.y & 1);
+  const int e = NCH == 2 ? blockIdx.y : blockIdx.y >> 1;
+  const int ch0 = NCH == 2 ? 0 : (blockIdx.y & 1);
   const int2 tt = a.tiles[blockIdx.x];
   const int ta = tt.x, tb = tt.y;
   const int nkb = a.Kp / BK;
@@ -212,7 +227,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 8) {
+  if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(512));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -221,120 +236,157 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-
   const int cbase = 2 * e + ch0;  // channel index of lc = 0
 
-  if (warp < 4) {
-    // ---------------- producers: one operand row per thread ----------------
-    const int r = tid;  // 0..127
+  if (warp < NPROD / 32) {
+    // ---------------- producers: two threads per operand row, 32 K each ----------------
+    const int r = tid & (BM - 1), half = tid >> 7;
     const float sB = a.sB[tb * BM + r];
-    float sA[2];
-    for (int lc = 0; lc < nch; lc++) sA[lc] = a.sA[(size_t)(cbase + lc) * a.Mp + ta * BM + r];
+    float sA[NCH];
+#pragma unroll
+    for (int lc = 0; lc < NCH; lc++) sA[lc] = a.sA[(size_t)(cbase + lc) * a.Mp + ta * BM + r];
     const float *ya = a.Yt + (size_t)(ta * BM + r) * a.Kp;
     const float *yb = a.Yt + (size_t)(tb * BM + r) * a.Kp;
     const float4 *wt = a.wt + (size_t)e * a.Kp;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
-      unsigned char *st = stage_base + (size_t)s * tiles_per_stage * TILE_BYTES;
+      unsigned char *st = stage_base + (size_t)s * TPS * TILE_BYTES;
       const int k0 = kb * BK;
 #pragma unroll 1
-      for (int c = 0; c < 8; c++) {  // 8 chunks of 8 K values (16 bytes of 16-bit values)
+      for (int cc = 0; cc < 4; cc++) {  // this thread's 4 chunks of 8 K values
+        const int c = 4 * half + cc;
         const float4 *pa = (const float4 *)(ya + k0 + 8 * c), *pb = (const float4 *)(yb + k0 + 8 * c);
         const float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), b0 = __ldg(pb), b1 = __ldg(pb + 1);
         const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
         const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-        uint16_t tbv[3][8], tav[2][3][8];
+        uint32_t wb[NP][4], wa[NCH][NP][4];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
           const float4 w = __ldg(wt + k0 + 8 * c + j);
-          const float wh[2] = {w.x, w.z}, wl[2] = {w.y, w.w};
-          uint16_t t[3];
-          split16(bv[j] * sB, 0.f, np, a.bf16, a.exact, t);
-          for (int p = 0; p < np; p++) tbv[p][j] = t[p];
-          for (int lc = 0; lc < nch; lc++) {
-            // (wh + wl) * y * s as a float pair: exact head product, error-free remainder
-            const float xs = wh[ch0 + lc] * sA[lc], xl = wl[ch0 + lc] * sA[lc];
+          uint16_t t[NP];
+          split_t<NP, EXACT, BF16>(bv[j] * sB, 0.f, t);
+#pragma unroll
+          for (int p = 0; p < NP; p++) {
+            if (j & 1) wb[p][j >> 1] |= (uint32_t)t[p] << 16;
+            else wb[p][j >> 1] = t[p];
+          }
+#pragma unroll
+          for (int lc = 0; lc < NCH; lc++) {
+            const int ch = ch0 + lc;
+            // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
+            const float xs = (ch == 0 ? w.x : w.z) * sA[lc], xl = (ch == 0 ? w.y : w.w) * sA[lc];
             const float zh = xs * av[j];
             const float zl = fmaf(xl, av[j], fmaf(xs, av[j], -zh));
-            split16(zh, zl, np, a.bf16, a.exact, t);
-            for (int p = 0; p < np; p++) tav[lc][p][j] = t[p];
+            split_t<NP, EXACT, BF16>(zh, zl, t);
+#pragma unroll
+            for (int p = 0; p < NP; p++) {
+              if (j & 1) wa[lc][p][j >> 1] |= (uint32_t)t[p] << 16;
+              else wa[lc][p][j >> 1] = t[p];
+            }
           }
         }
         const uint32_t off = swz(r, c);
-        for (int p = 0; p < np; p++) {
-          uint4 v;
-          v.x = tbv[p][0] | ((uint32_t)tbv[p][1] << 16); v.y = tbv[p][2] | ((uint32_t)tbv[p][3] << 16);
-          v.z = tbv[p][4] | ((uint32_t)tbv[p][5] << 16); v.w = tbv[p][6] | ((uint32_t)tbv[p][7] << 16);
-          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = v;  // B planes first
-          for (int lc = 0; lc < nch; lc++) {
-            const uint16_t *t = tav[lc][p];
-            v.x = t[0] | ((uint32_t)t[1] << 16); v.y = t[2] | ((uint32_t)t[3] << 16);
-            v.z = t[4] | ((uint32_t)t[5] << 16); v.w = t[6] | ((uint32_t)t[7] << 16);
-            *(uint4 *)(st + (size_t)(np * (1 + lc) + p) * TILE_BYTES + off) = v;  // then A planes per channel
-          }
+#pragma unroll
+        for (int p = 0; p < NP; p++) {
+          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = make_uint4(wb[p][0], wb[p][1], wb[p][2], wb[p][3]);
+#pragma unroll
+          for (int lc = 0; lc < NCH; lc++)
+            *(uint4 *)(st + (size_t)(NP * (1 + lc) + p) * TILE_BYTES + off) =
+                make_uint4(wa[lc][p][0], wa[lc][p][1], wa[lc][p][2], wa[lc][p][3]);
         }
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
     }
-  } else if (warp < 8) {
-    // ---------------- epilogue: drain FP32 sub-chunk sums into FP64 ----------------
-    const int q = warp - 4;                 // this warp may read TMEM lanes 32q..32q+31
+  } else if (warp < MMA_WARP) {
+    // ---------------- epilogue: fold each sub-chunk into a float-pair accumulator ----------------
+    // TMEM columns per channel: [main][corr (exact scheme)][acc hi][acc lo], 128 each.
+    // acc = hi + lo is updated with an error-free TwoSum, so the running sum keeps
+    // about 48 bits with FP32 arithmetic only; the FP64 tile is written once.
+    const int q = warp & 3;                 // this warp may read TMEM lanes 32q..32q+31
     const int row = ta * BM + 32 * q + lane;
-    const int nacc = a.exact ? 2 : 1;
+    const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
     for (int sc = 0; sc < nsub; sc++) {
-      const int b = sc & 1, use = sc >> 1;
-      if (!mbar_wait(&accfull[b], use & 1, abort_flag)) break;
+      if (!mbar_wait(&accfull[0], sc & 1, abort_flag)) break;
       tc_fence_after();
-      for (int lc = 0; lc < nch; lc++) {
+#pragma unroll 1
+      for (int lc = 0; lc < NCH; lc++) {
+        const uint32_t cm = (uint32_t)(lc * (NACC + 2)) * BN, cc = cm + BN, ch = cm + NACC * BN, cl = ch + BN;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          float m[16], cr[16], hi[16], lo[16];
+          tmem_ld16(lanebase + cm + c0, m);
+          if (NACC == 2) tmem_ld16(lanebase + cc + c0, cr);
+          if (sc > 0) { tmem_ld16(lanebase + ch + c0, hi); tmem_ld16(lanebase + cl + c0, lo); }
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const float a0 = sc > 0 ? hi[j] : 0.f, l0 = sc > 0 ? lo[j] : 0.f;
+            const float x = m[j];
+            const float sm = a0 + x, bb = sm - a0;
+            const float err = (a0 - (sm - bb)) + (x - bb);
+            hi[j] = sm;
+            lo[j] = l0 + err + (NACC == 2 ? cr[j] : 0.f);
+          }
+          tmem_st16(lanebase + ch + c0, hi);
+          tmem_st16(lanebase + cl + c0, lo);
+        }
+      }
+      tmem_wait_st();
+      tc_fence_before();
+      mbar_arrive(&accempty[0]);
+    }
+    // the batch's sum, unscaled, into the FP64 tile
+    if (!*abort_flag) {
+      tc_fence_after();
+#pragma unroll 1
+      for (int lc = 0; lc < NCH; lc++) {
+        const uint32_t ch = (uint32_t)(lc * (NACC + 2) + NACC) * BN, cl = ch + BN;
         const double ia = 1.0 / (double)a.sA[(size_t)(cbase + lc) * a.Mp + row];
         double *dst = a.M64 + (((size_t)e * 2 + ch0 + lc) * a.Mp + row) * a.Mp + tb * BN;
         const float *sbc = a.sB + tb * BN;
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-          float v[32], w[32];
-          const uint32_t col = (uint32_t)(((b * nch + lc) * nacc) * BN + c0);
-          tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col, v);
-          if (nacc == 2) tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + col + BN, w);
-#pragma unroll 4
-          for (int j = 0; j < 32; j++) {
-            const double s = nacc == 2 ? (double)v[j] + (double)w[j] : (double)v[j];
-            dst[c0 + j] += s * ia / (double)sbc[c0 + j];
-          }
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+          float hi[16], lo[16];
+          tmem_ld16(lanebase + ch + c0, hi);
+          tmem_ld16(lanebase + cl + c0, lo);
+          tmem_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 16; j++) dst[c0 + j] += ((double)hi[j] + (double)lo[j]) * ia / (double)sbc[c0 + j];
         }
       }
-      tc_fence_before();
-      mbar_arrive(&accempty[b]);
     }
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
-    const uint32_t idesc = make_idesc(a.bf16, BM, BN);
-    int kb = 0;
+    const uint32_t idesc = make_idesc(BF16 ? 1 : 0, BM, BN);
     for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
-      const int b = sc & 1, buse = sc >> 1;
-      if (buse > 0 && !mbar_wait(&accempty[b], (buse - 1) & 1, abort_flag)) break;
+      // the epilogue must have read the previous sub-chunk's sums
+      if (sc > 0 && !mbar_wait(&accempty[0], (sc - 1) & 1, abort_flag)) break;
       tc_fence_after();
       const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
       bool ok = true;
-      for (kb = kbeg; kb < kend; kb++) {
+      for (int kb = kbeg; kb < kend; kb++) {
         const int s = kb & 1, use = kb >> 1;
         if (!mbar_wait(&full[s], use & 1, abort_flag)) { ok = false; break; }
         tc_fence_after();
-        const uint32_t st = smem_u32(stage_base + (size_t)s * tiles_per_stage * TILE_BYTES);
-        const int nacc = a.exact ? 2 : 1;
+        const uint32_t st = smem_u32(stage_base + (size_t)s * TPS * TILE_BYTES);
+#pragma unroll
         for (int kk = 0; kk < BK / 16; kk++)
-          for (int lc = 0; lc < nch; lc++) {
-            const uint32_t d0 = tmem + (uint32_t)(((b * nch + lc) * nacc) * BN);
+#pragma unroll
+          for (int lc = 0; lc < NCH; lc++) {
+            const uint32_t d0 = tmem + (uint32_t)(lc * (NACC + 2)) * BN;
             const bool fresh = (kb == kbeg && kk == 0);
             int idx0 = 0, idx1 = 0;
-            // products of planes pa (A) and pb (B) with pa + pb <= np - 1; with the
+            // products of planes pa (A) and pb (B) with pa + pb <= NP - 1; with the
             // exact scheme the leading product has its own accumulator
-            for (int pa = 0; pa < np; pa++)
-              for (int pb = 0; pa + pb < np; pb++) {
-                const uint64_t ad = make_desc(st + (uint32_t)((np * (1 + lc) + pa) * TILE_BYTES) + kk * 32);
+#pragma unroll
+            for (int pa = 0; pa < NP; pa++)
+#pragma unroll
+              for (int pb = 0; pa + pb < NP; pb++) {
+                const uint64_t ad = make_desc(st + (uint32_t)((NP * (1 + lc) + pa) * TILE_BYTES) + kk * 32);
                 const uint64_t bd = make_desc(st + (uint32_t)(pb * TILE_BYTES) + kk * 32);
-                const bool lead = nacc == 2 && pa == 0 && pb == 0;
-                if (lead || nacc == 1) {
+                if ((EXACT && pa == 0 && pb == 0) || !EXACT) {
                   mma_f16(d0, ad, bd, idesc, (fresh && idx0 == 0) ? 0 : 1);
                   idx0++;
                 } else {
@@ -346,7 +398,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
         mma_commit(&empty[s]);
       }
       if (!ok) break;
-      mma_commit(&accfull[b]);
+      mma_commit(&accfull[0]);
     }
     // wait for every MMA this thread issued before tensor memory is released
     mma_commit(fin);
@@ -356,7 +408,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   if (tid == 0 && *abort_flag) atomicExch(a.err, 4);
   tc_fence_before();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == MMA_WARP) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
@@ -511,7 +563,10 @@ __global__ void assemble_kernel(const double *__restrict__ M64, int Mp, int Gp, 
 void TcWorkspace::release() {
   if (planes) cudaFree(planes);
   if (part) cudaFree(part);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
   planes = part = nullptr;
+  ev0 = ev1 = nullptr;
   planes_bytes = part_bytes = 0;
 }
 
@@ -529,6 +584,8 @@ static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
 
 void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st) {
   ws.ng = ng; ws.nen = nen; ws.ndir = ndir;
+  ws.gram_seconds = 0;
+  if (!ws.ev0) { RP_CUDA(cudaEventCreate(&ws.ev0)); RP_CUDA(cudaEventCreate(&ws.ev1)); }
   const int Mp = 2 * Gp_of(ng);
   const size_t mbytes = sizeof(double) * (size_t)nen * 2 * Mp * Mp;
   grow(ws.part, ws.part_bytes, mbytes);
@@ -587,23 +644,31 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
   a.exact = exact;
   a.sB = sBv; a.sA = sAv;
-  // two accumulators per channel in the exact scheme: one channel per CTA keeps
-  // double-buffered accumulators within the 512 TMEM columns
-  a.nch = (a.nplanes == 2 && !exact) ? 2 : 1;
-  // default 512 K per FP32 sub-chunk: the correction accumulator's rounding
-  // bias grows with its length; integer partial sums must stay below 2^24
-  a.ksub_blocks = ws.ksub > 0 ? ws.ksub : 8;
+  // one channel per CTA: main (+ correction) accumulators and the float-pair
+  // running sum take 3 or 4 x 128 of the 512 TMEM columns
+  a.nch = 1;
+  // default 1024 K per FP32 sub-chunk: integer partial sums must stay below 2^24
+  a.ksub_blocks = ws.ksub > 0 ? ws.ksub : 16;
   if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
   const int tiles_per_stage = a.nplanes * (1 + a.nch);
   const size_t smem = 1024 + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES + 128;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
-  RP_CUDA(cudaFuncSetAttribute(tc_gram_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  void (*kern)(TcArgs);
+  if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, 1, true, false>;
+  else if (precision == RP_PREC_BF16X3) kern = tc_gram_kernel<3, 1, true, true>;
+  else kern = tc_gram_kernel<2, 1, false, false>;
+  RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((unsigned)tl.size(), nen * (2 / a.nch));
-  tc_gram_kernel<<<grid, NTHREADS, smem, st>>>(a);
+  RP_CUDA(cudaEventRecord(ws.ev0, st));
+  kern<<<grid, NTHREADS, smem, st>>>(a);
+  RP_CUDA(cudaEventRecord(ws.ev1, st));
   launches++;
   RP_CUDA(cudaGetLastError());
   RP_CUDA(cudaStreamSynchronize(st));  // the workspace (and tile list) is reused by the next batch
+  float ms = 0;
+  RP_CUDA(cudaEventElapsedTime(&ms, ws.ev0, ws.ev1));
+  ws.gram_seconds += ms * 1e-3;
   return launches;
 }
 

@@ -14,6 +14,8 @@ struct TcWorkspace {
   size_t part_bytes = 0;
   int ng = 0, nen = 0, ndir = 1;
   int ksub = 16;          // K blocks per FP32 accumulation
+  double gram_seconds = 0;  // device time of the Gram kernel in the current q
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   size_t bytes() const { return planes_bytes + part_bytes; }
   void release();
 };

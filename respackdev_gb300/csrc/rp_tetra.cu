@@ -1,5 +1,4 @@
-// rp_tetra.cu -- generalized tetrahedron weights in FP64 (K4), built with
-// --fmad=false so the closed forms round like the reference's.
+// rp_tetra.cu -- generalized tetrahedron weights in FP64 (K4).
 //
 // Follows src/chiqw/m_tetrahedron_20170325.F (MIT-licensed Fujiwara et al.
 // generalized tetrahedron method): ttrhdrn_chi0 (:99-141) splits every
@@ -273,13 +272,73 @@ __device__ bool tetra_terms(double dmna, double dmnr, const cx *ffk, const cx *g
   return true;
 }
 
+// Normal case (no near-degenerate vertices) of calc() with shared vertex logs.
+// All four g share the imaginary part delt*dsgn, so d_ab = g_a - g_b is real and
+// log(z_a / z_b) = L_a - L_b with L = log(g + w) (z_a, z_b in the same half
+// plane).  The closed forms of sub2normal / sub1normal (:346-363, :435-451) then
+// need only real reciprocal differences, shared across frequencies.
+struct NormalCoef {
+  double A[3], B[3], C[3], D[3];   // the three sub2normal forms
+  double S1a, S1b, S1c;            // sub1normal
+  int p[3], q[3], r[3], s[3];
+  int a0, a1, a2, a3;
+};
+
+__device__ __forceinline__ void normal_coef(const double *gr, const int *a, NormalCoef &c) {
+  double id[4][4];
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) id[i][j] = (i == j) ? 0.0 : 1.0 / (gr[i] - gr[j]);
+  c.a0 = a[0]; c.a1 = a[1]; c.a2 = a[2]; c.a3 = a[3];
+  // c1 = sub2normal(g[a1], g[a0], g[a2], g[a3]), c2 = sub2normal(a0, a1, a2, a3), c3 = sub2normal(a0, a2, a1, a3)
+  const int P[3] = {a[1], a[0], a[0]}, Q[3] = {a[0], a[1], a[2]}, R[3] = {a[2], a[2], a[1]}, S[3] = {a[3], a[3], a[3]};
+  for (int f = 0; f < 3; f++) {
+    const int p = P[f], q = Q[f], r = R[f], s = S[f];
+    c.p[f] = p; c.q[f] = q; c.r[f] = r; c.s[f] = s;
+    c.A[f] = id[p][q] * id[q][r] * id[q][s] / 6.0;
+    c.B[f] = id[p][r] * id[q][r] * id[q][r] * id[r][s] / 6.0;
+    c.C[f] = id[p][s] * id[q][s] * id[q][s] * id[r][s] / 6.0;
+    c.D[f] = id[p][q] * id[p][q] * id[p][r] * id[p][s] / 6.0;
+  }
+  // c4 = sub1normal(g0 = a0, g1 = a3, g2 = a1, g3 = a2)
+  const int p = a[0], q = a[3], r = a[1], s = a[2];
+  c.S1a = 0.5 * id[p][r] * id[p][s] * id[p][q];
+  c.S1b = 0.5 * id[p][r] * id[q][r] * id[r][s];
+  c.S1c = 0.5 * id[q][s] * id[p][s] * id[r][s];
+}
+
+// vertex terms for one frequency given z_a = g_a + w, z^2, z^3 and L_a = log z_a
+__device__ __forceinline__ void normal_terms(const NormalCoef &c, const cx *z2, const cx *z3, const cx *L,
+                                             const cx *fk, cx *x) {
+  cx F[3];
+  for (int f = 0; f < 3; f++) {
+    const int p = c.p[f], q = c.q[f], r = c.r[f], s = c.s[f];
+    F[f] = -(z2[q] * c.A[f]) - z3[r] * (L[r] - L[q]) * c.B[f] + z3[s] * (L[s] - L[q]) * c.C[f] +
+           z3[p] * (L[p] - L[q]) * c.D[f];
+  }
+  const int p = c.a0, q = c.a3, r = c.a1, s = c.a2;
+  const cx lq = z2[q] * (L[q] - L[p]), lr = z2[r] * (L[r] - L[p]), ls = z2[s] * (L[s] - L[p]);
+  const cx F4 = -(lq * c.S1a) - (lq - lr) * c.S1b + (lq - ls) * c.S1c;
+  x[c.a0] = fk[c.a0] * F[0];
+  x[c.a1] = fk[c.a1] * F[1];
+  x[c.a2] = fk[c.a2] * F[2];
+  x[c.a3] = fk[c.a3] * (F4 - F[2] - F[1] - F[0]);
+}
+
+// Tetrahedra are first sorted into shared-memory lists by the work they need --
+// normal (the shared-log closed forms), near-degenerate (the reference's special
+// forms) and Fermi-cut (ttct) -- so the threads of a warp run the same code.
 __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec, double2 *__restrict__ wout) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int p = blockIdx.x, e0 = blockIdx.y * nec, ntk = a.ntk;
   const int ne = min(nec, a.nen - e0);
+  const int ntet = 6 * ntk;
   double2 *xo = (double2 *)smem;               // ntk * nec
-  double *e1m = (double *)(xo + (size_t)ntk * nec), *e2m = e1m + ntk;
+  double2 *Lt = xo + (size_t)ntk * nec;        // [sign][mesh slot][e] log(g + w)
+  double *e1m = (double *)(Lt + 2 * (size_t)ntk * nec), *e2m = e1m + ntk;
+  int *lists = (int *)(e2m + ntk);             // 2*ntet entries: normal from the front, others from the back
+  __shared__ int n_normal, n_other;
   const int bv = a.pair_vir[p], bo = a.pair_occ[p];
+  if (threadIdx.x == 0) { n_normal = 0; n_other = 0; }
   for (int i = threadIdx.x; i < ntk * nec; i += blockDim.x) xo[i] = make_double2(0, 0);
   for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
     int k = a.index_kpt[m];
@@ -288,54 +347,113 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
   }
   __syncthreads();
   const double f = a.efermi, delt = a.delt;
-  for (int t = threadIdx.x; t < 6 * ntk; t += blockDim.x) {
+  // log(g_k + w) per mesh vertex, sign and frequency of the chunk
+  for (int i = threadIdx.x; i < 2 * ntk * ne; i += blockDim.x) {
+    const int sg = i / (ntk * ne), rem = i % (ntk * ne), m = rem / ne, e = rem % ne;
+    const double dsgn = sg == 0 ? 1.0 : -1.0;
+    const cx g = cx(-(e2m[m] - e1m[m]), delt) * dsgn;
+    const cx z = g + cx(a.em[e0 + e].x, a.em[e0 + e].y);
+    const cx L = clog_(z);
+    Lt[((size_t)sg * ntk + m) * nec + e] = make_double2(L.r, L.i);
+  }
+  // classify (tetrahedron, sign): code = 2*t + sg
+  for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
+    double ee1[4], ee2[4];
+    for (int v = 0; v < 4; v++) { const int sl = a.imt1[4 * t + v]; ee1[v] = e1m[sl]; ee2[v] = e2m[sl]; }
+    const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
+    const double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
+    const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
+    if (mx2 <= f) continue;  // ttct(+1) drops the whole tetrahedron
+    const bool uncut = mn2 > f && mx1 < f;
+    for (int sg = 0; sg < 2; sg++) {
+      bool normal = false;
+      if (uncut) {
+        const double dsgn = sg == 0 ? 1.0 : -1.0;
+        cx ggk[4];
+        for (int v = 0; v < 4; v++) ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
+        normal = chk1(a.dmna, a.dmnr, ggk).s == 0;
+      }
+      if (normal) lists[atomicAdd(&n_normal, 1)] = 2 * t + sg;
+      else lists[2 * ntet - 1 - atomicAdd(&n_other, 1)] = 2 * t + sg;
+    }
+  }
+  __syncthreads();
+  // normal tetrahedra: shared logs, real reciprocal differences
+  for (int idx = threadIdx.x; idx < n_normal; idx += blockDim.x) {
+    const int code = lists[idx], t = code >> 1, sg = code & 1;
+    const double dsgn = sg == 0 ? 1.0 : -1.0;
+    int slot[4];
+    cx ffk[4], ggk[4];
+    double gr[4];
+    for (int v = 0; v < 4; v++) {
+      slot[v] = a.imt1[4 * t + v];
+      ffk[v] = cx(dsgn, 0);
+      ggk[v] = cx(-(e2m[slot[v]] - e1m[slot[v]]), delt) * dsgn;
+      gr[v] = ggk[v].r;
+    }
+    const Chk c = chk1(a.dmna, a.dmnr, ggk);
+    NormalCoef nc;
+    normal_coef(gr, c.ia4, nc);
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      cx x[4];
+      if (ggk[0].i + w.i == 0.0) {
+        // z on the real axis: keep the ratio logs of the reference
+        if (!calc_w(c, ffk, ggk, w, x)) { atomicExch(a.err, 2); continue; }
+      } else {
+        cx z2[4], z3[4], L[4];
+        for (int v = 0; v < 4; v++) {
+          const cx z = ggk[v] + w;
+          z2[v] = z * z;
+          z3[v] = z2[v] * z;
+          const double2 l = Lt[((size_t)sg * ntk + slot[v]) * nec + e];
+          L[v] = cx(l.x, l.y);
+        }
+        normal_terms(nc, z2, z3, L, ffk, x);
+      }
+      for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], x[v]);
+    }
+  }
+  // near-degenerate or Fermi-cut tetrahedra: the reference's forms
+  for (int idx = threadIdx.x; idx < n_other; idx += blockDim.x) {
+    const int code = lists[2 * ntet - 1 - idx], t = code >> 1, sg = code & 1;
+    const double dsgn = sg == 0 ? 1.0 : -1.0;
     int slot[4];
     double ee1[4], ee2[4];
     for (int v = 0; v < 4; v++) { slot[v] = a.imt1[4 * t + v]; ee1[v] = e1m[slot[v]]; ee2[v] = e2m[slot[v]]; }
-    double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
-    double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
-    double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
-    if (mx2 <= f) continue;  // ttct(+1) drops the whole tetrahedron
-    for (int sg = 0; sg < 2; sg++) {
-      const double dsgn = sg == 0 ? 1.0 : -1.0;
-      if (mn2 > f && mx1 < f) {
-        // not cut: one piece, identity weights, volume 1
-        cx ffk[4], ggk[4];
-        for (int v = 0; v < 4; v++) {
-          ffk[v] = cx(dsgn, 0);
-          ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
-        }
-        if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, nullptr, xo)) atomicExch(a.err, 2);
-        continue;
+    const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
+    const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
+    if (mn2 > f && mx1 < f) {
+      cx ffk[4], ggk[4];
+      for (int v = 0; v < 4; v++) { ffk[v] = cx(dsgn, 0); ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn; }
+      if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, nullptr, xo)) atomicExch(a.err, 2);
+      continue;
+    }
+    double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
+    for (int i = 0; i < 4; i++)
+      for (int v = 0; v < 4; v++) dwgt[0][i][v] = (i == v) ? 1.0 : 0.0;
+    dvol[0] = 1.0;
+    int nt = 1;
+    if (!ttct(f, ee2, +1, nt, dwgt, dvol) || !ttct(f, ee1, -1, nt, dwgt, dvol)) { atomicExch(a.err, 1); continue; }
+    for (int i3 = 0; i3 < nt; i3++) {
+      cx ffk[4], ggk[4];
+      for (int i4 = 0; i4 < 4; i4++) {
+        double sm = 0;
+        for (int v = 0; v < 4; v++) sm += (ee2[v] - ee1[v]) * dwgt[i3][i4][v];
+        ffk[i4] = cx(dvol[i3], 0) * dsgn;
+        ggk[i4] = cx(-sm, delt) * dsgn;
       }
-      double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
-      for (int i = 0; i < 4; i++)
-        for (int v = 0; v < 4; v++) dwgt[0][i][v] = (i == v) ? 1.0 : 0.0;
-      dvol[0] = 1.0;
-      int ntet = 1;
-      if (!ttct(f, ee2, +1, ntet, dwgt, dvol) || !ttct(f, ee1, -1, ntet, dwgt, dvol)) { atomicExch(a.err, 1); continue; }
-      for (int i3 = 0; i3 < ntet; i3++) {
-        cx ffk[4], ggk[4];
-        for (int i4 = 0; i4 < 4; i4++) {
-          double s = 0;
-          for (int v = 0; v < 4; v++) s += (ee2[v] - ee1[v]) * dwgt[i3][i4][v];
-          ffk[i4] = cx(dvol[i3], 0) * dsgn;
-          ggk[i4] = cx(-s, delt) * dsgn;
-        }
-        double w4[4][4];
-        for (int i4 = 0; i4 < 4; i4++)
-          for (int v = 0; v < 4; v++) w4[i4][v] = dwgt[i3][i4][v];
-        if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, w4, xo)) atomicExch(a.err, 2);
-      }
+      double w4[4][4];
+      for (int i4 = 0; i4 < 4; i4++)
+        for (int v = 0; v < 4; v++) w4[i4][v] = dwgt[i3][i4][v];
+      if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, w4, xo)) atomicExch(a.err, 2);
     }
   }
   __syncthreads();
   // w[(p*nen + e)*ntk + k] = xow(mesh(k), e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
   for (int i = threadIdx.x; i < ntk * ne; i += blockDim.x) {
     const int e = i / ntk, k = i % ntk;
-    int m = 0;
-    // mesh slot of k: index_kpt is a permutation; invert it via a scan-free lookup
-    m = a.index_kpt[ntk + k];  // second half holds the inverse map
+    const int m = a.index_kpt[ntk + k];  // second half holds k -> mesh slot
     double2 x = xo[(size_t)m * nec + e];
     double2 po = a.prob[(size_t)k * a.ntb + bo], pv = a.prob[(size_t)a.kpq[k] * a.ntb + bv];
     double2 pp = make_double2(1.0 - (po.x * pv.x - po.y * pv.y), -(po.x * pv.y + po.y * pv.x));
@@ -346,10 +464,12 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
 
 int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st) {
   if (a.npair == 0) return 0;
+  // weights (ntk x nec) and vertex logs (2 x ntk x nec) of a frequency chunk in shared memory
   int nec = a.nen;
-  const size_t budget = 180 * 1024 - 16 * (size_t)a.ntk;
-  while (nec > 1 && (size_t)a.ntk * nec * sizeof(double2) > budget) nec = (nec + 1) / 2;
-  size_t smem = (size_t)a.ntk * nec * sizeof(double2) + 2 * sizeof(double) * a.ntk;
+  const size_t fixed = 2 * sizeof(double) * (size_t)a.ntk + 2 * 6 * sizeof(int) * (size_t)a.ntk;
+  const size_t budget = 210 * 1024 - fixed;
+  while (nec > 1 && (size_t)a.ntk * nec * 3 * sizeof(double2) > budget) nec--;
+  size_t smem = (size_t)a.ntk * nec * 3 * sizeof(double2) + fixed;
   if (smem > 227 * 1024) fail(1, "k mesh too large for the tetrahedron tile (%zu bytes)", smem);
   RP_CUDA(cudaFuncSetAttribute(tetra_weights_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(a.npair, (a.nen + nec - 1) / nec);
