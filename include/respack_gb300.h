@@ -137,6 +137,28 @@ long long rp_kernel_launches(const rp_ctx *ctx);
 const char *rp_last_error(const rp_ctx *ctx);
 void rp_ctx_destroy(rp_ctx *ctx);
 
+/* Batched inverse of nmat complex n x n matrices (column-major, interleaved
+ * re/im doubles, matrix m at a + 2*m*n*n) that allocates no device memory.
+ * No counterpart in the reference: it is the inversion step of rp_epsinv_q
+ * (invZGE.F90:1-22, partial pivoting on |re|+|im|) offered on its own for
+ * callers that cannot allocate GPU memory or let a library do so -- a Fortran
+ * or C++ host whose device memory belongs to its own allocator or pool, or
+ * code that runs where cudaMalloc is not allowed.  a and ainv are device
+ * pointers, 16-byte aligned; a == ainv inverts in place, otherwise a is left
+ * unchanged.  The work is queued on `stream` (a cudaStream_t, NULL = legacy
+ * default stream) and the call returns after that stream has finished it.
+ *
+ * Scratch lives in one fixed device array of the library (about 4.6 MB per
+ * GPU, allocated when the library is loaded): n*nmat <= 131072 and
+ * nmat <= 1024, larger requests are rejected with code 1 before any work.
+ * Nothing in it has to start at zero; the error word is cleared by each call.
+ * The first call on each device looks the array up (cudaGetSymbolAddress) with
+ * that device current; make it before any stream capture.  Calls whose work
+ * overlaps on the GPU (different streams or host threads) share the array and
+ * race: serialise them.  Returns 0, 1 (bad arguments or size), 3 (singular
+ * matrix) or -1 (CUDA error); rp_last_error(NULL) gives the text. */
+int rp_zinv_batched_noalloc(const double *a, double *ainv, int n, int nmat, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,9 @@ struct rp_ctx {
 
 static thread_local std::string g_create_err;
 
+// error text of calls that have no context (read by rp_last_error(NULL))
+void rp::set_global_error(const std::string &msg) { g_create_err = msg; }
+
 template <typename F> static int guarded(rp_ctx *ctx, F &&f) {
   try {
     f();

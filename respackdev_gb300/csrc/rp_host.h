@@ -28,6 +28,7 @@ struct Error : std::exception {
   const char *what() const noexcept override { return msg.c_str(); }
 };
 [[noreturn]] void fail(int code, const char *fmt, ...);
+void set_global_error(const std::string &msg);  // text of rp_last_error(NULL)
 
 // ---- Fortran list-directed text and unformatted sequential files ----------
 class ListReader {
