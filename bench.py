@@ -259,13 +259,14 @@ def run_gpu(args):
         # --- end to end through the C ABI with host buffers ---
         ng, nen = ctx.ng, info.nen
         e2e_steps = max(1, min(args.steps, 3))
+        h2d0, d2h0 = ctx.transfer_bytes()
         t0 = time.perf_counter()
         for iq in mine[args.warmup: args.warmup + e2e_steps]:
             ctx.chi0_q(iq, fetch=True)
             ctx.epsinv_q(fetch=True)
         e2e = (time.perf_counter() - t0) / e2e_steps
-        d2h = 2 * ng * ng * nen * 16
-        h2d = ng * 3 * 4 + info.ntk * 4 * 4 + 2 * 1536 * 4
+        h2d1, d2h1 = ctx.transfer_bytes()
+        h2d, d2h = (h2d1 - h2d0) // e2e_steps, (d2h1 - d2h0) // e2e_steps
         # --- plain FP64 path and the error of the fast path on a pair sample of one q ---
         npair_full = info.n_occ * info.n_vir
         iq0 = mine[args.warmup]

@@ -134,6 +134,10 @@ int rp_stage_times(const rp_ctx *ctx, double *t6);
 /* Number of kernel launches issued by this context so far. */
 long long rp_kernel_launches(const rp_ctx *ctx);
 
+/* Bytes this context's calls copied host->device and device->host so far
+ * (task tables, Gamma rows, results fetched into host buffers). */
+int rp_transfer_bytes(const rp_ctx *ctx, long long *h2d, long long *d2h);
+
 const char *rp_last_error(const rp_ctx *ctx);
 void rp_ctx_destroy(rp_ctx *ctx);
 

@@ -80,6 +80,10 @@ def load() -> C.CDLL:
     L.rp_q_dims.restype = C.c_int
     L.rp_kernel_launches.argtypes = [vp]
     L.rp_kernel_launches.restype = C.c_longlong
+    L.rp_transfer_bytes.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.rp_transfer_bytes.restype = C.c_int
+    L.rp_zinv_batched_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, vp]
+    L.rp_zinv_batched_noalloc.restype = C.c_int
     L.rp_last_error.argtypes = [vp]
     L.rp_last_error.restype = C.c_char_p
     L.rp_ctx_destroy.argtypes = [vp]
@@ -186,6 +190,12 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.L.rp_kernel_launches(self._h))
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes copied by this context's calls so far."""
+        h, d = C.c_longlong(0), C.c_longlong(0)
+        self.L.rp_transfer_bytes(self._h, C.byref(h), C.byref(d))
+        return int(h.value), int(d.value)
 
     def close(self):
         if self._h:

@@ -43,9 +43,14 @@ struct DevBuf {
   void release() { if (p) cudaFree(p); p = nullptr; bytes = 0; }
 };
 
+// bytes copied host->device and device->host by the calling thread; the C-ABI
+// calls add the change over each call to their context's totals
+thread_local long long t_h2d = 0, t_d2h = 0;
+
 template <typename T> void upload(DevBuf &b, const std::vector<T> &v, cudaStream_t st) {
   b.ensure(std::max<size_t>(sizeof(T) * v.size(), 16));
   if (!v.empty()) RP_CUDA(cudaMemcpyAsync(b.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+  t_h2d += (long long)(sizeof(T) * v.size());
 }
 
 }  // namespace
@@ -72,6 +77,7 @@ struct rp_ctx {
   std::vector<cd> h_chi, h_eps;
   cudaEvent_t ev[6]{};
   double times[6]{};
+  long long h2d = 0, d2h = 0;  // bytes moved between host and device by this context's calls
   ~rp_ctx() {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
@@ -88,8 +94,14 @@ static thread_local std::string g_create_err;
 
 // error text of calls that have no context (read by rp_last_error(NULL))
 void rp::set_global_error(const std::string &msg) { g_create_err = msg; }
+void rp::note_transfer(long long h2d, long long d2h) { t_h2d += h2d; t_d2h += d2h; }
 
 template <typename F> static int guarded(rp_ctx *ctx, F &&f) {
+  const long long h0 = t_h2d, d0 = t_d2h;
+  struct Count {
+    rp_ctx *c; long long h0, d0;
+    ~Count() { if (c) { c->h2d += t_h2d - h0; c->d2h += t_d2h - d0; } }
+  } count{ctx, h0, d0};
   try {
     f();
     return 0;
@@ -106,6 +118,7 @@ static void check_device_error(rp_ctx *c) {
   int e = 0;
   RP_CUDA(cudaMemcpyAsync(&e, c->errw.p, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   RP_CUDA(cudaStreamSynchronize(c->st));
+  t_d2h += sizeof(int);
   if (e == 1) rp::fail(-3, "ntet.gt.nmax: a tetrahedron was cut into too many pieces");
   if (e == 2) rp::fail(-3, "tetrahedron degeneracy classification failed (bad i3 / bad sum ia2)");
   if (e == 3) rp::fail(-3, "dielectric matrix is singular");
@@ -311,6 +324,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
     RP_CUDA(cudaMemcpyAsync(chi + 2 * m, chi, sizeof(cd) * m, cudaMemcpyDeviceToDevice, st));
     std::vector<cd> rc(4 * (size_t)nen * ng);
     RP_CUDA(cudaMemcpyAsync(rc.data(), c->rowcol.p, sizeof(cd) * rc.size(), cudaMemcpyDeviceToHost, st));
+    t_d2h += (long long)(sizeof(cd) * rc.size());
     RP_CUDA(cudaStreamSynchronize(st));
     for (int ix = 1; ix <= 2; ix++)
       for (int e = 0; e < nen; e++) {
@@ -322,6 +336,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
         RP_CUDA(cudaMemcpy2DAsync(base + t.no_g0, sizeof(double2) * ng, rr.data(), sizeof(double2), sizeof(double2), ng,
                                   cudaMemcpyHostToDevice, st));
         RP_CUDA(cudaMemcpyAsync(base + (size_t)ng * t.no_g0, cl.data(), sizeof(double2) * ng, cudaMemcpyHostToDevice, st));
+        t_h2d += (long long)(2 * sizeof(double2) * ng);
         RP_CUDA(cudaStreamSynchronize(st));
       }
   }
@@ -343,6 +358,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
                                         (int)t.intra_band.size(), c->pwpl.as<double2>(), st);
     cd pw[3];
     RP_CUDA(cudaMemcpyAsync(pw, c->pwpl.p, sizeof(cd) * 3, cudaMemcpyDeviceToHost, st));
+    t_d2h += (long long)(sizeof(cd) * 3);
     RP_CUDA(cudaStreamSynchronize(st));
     for (int d = 0; d < 3; d++) {
       cd wpl = 8.0 * pw[d] / S.volume / (double)ntk;
@@ -391,6 +407,7 @@ static void fetch(rp_ctx *c, DevBuf &b, std::vector<cd> &h) {
   h.resize((size_t)c->ndir * c->S.em.size() * t.ng * t.ng);
   RP_CUDA(cudaMemcpyAsync(h.data(), b.p, sizeof(cd) * h.size(), cudaMemcpyDeviceToHost, c->st));
   RP_CUDA(cudaStreamSynchronize(c->st));
+  t_d2h += (long long)(sizeof(cd) * h.size());
 }
 
 static void mkdir_p(const std::string &p) { mkdir(p.c_str(), 0755); }
@@ -527,6 +544,13 @@ int rp_q_dims(const rp_ctx *c, int iq, int *ng, int *ndir) {
 }
 
 long long rp_kernel_launches(const rp_ctx *c) { return c ? c->launches : 0; }
+
+int rp_transfer_bytes(const rp_ctx *c, long long *h2d, long long *d2h) {
+  if (!c) return 1;
+  if (h2d) *h2d = c->h2d;
+  if (d2h) *d2h = c->d2h;
+  return 0;
+}
 
 const char *rp_last_error(const rp_ctx *c) { return c ? c->err.c_str() : g_create_err.c_str(); }
 

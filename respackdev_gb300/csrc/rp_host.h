@@ -29,6 +29,8 @@ struct Error : std::exception {
 };
 [[noreturn]] void fail(int code, const char *fmt, ...);
 void set_global_error(const std::string &msg);  // text of rp_last_error(NULL)
+// count bytes a helper copied between host and device for the calling context
+void note_transfer(long long h2d, long long d2h);
 
 // ---- Fortran list-directed text and unformatted sequential files ----------
 class ListReader {

@@ -637,6 +637,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   static thread_local size_t d_tiles_bytes = 0;
   grow(d_tiles, d_tiles_bytes, sizeof(int2) * tl.size());
   RP_CUDA(cudaMemcpyAsync(d_tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, st));
+  note_transfer((long long)(sizeof(int2) * tl.size()), 0);
   TcArgs a;
   a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.M64 = (double *)ws.part; a.err = err;
   a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;

@@ -56,6 +56,31 @@ def _from_device(t, ng: int, nmat: int) -> np.ndarray:
 
 
 @pytest.mark.gpu
+def test_noalloc_reports_singular_input():
+    """A matrix with a zero column gives code 3; the next call works again."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    L = _lib()
+    n, nmat = 6, 2
+    rng = np.random.default_rng(3)
+    m = rng.standard_normal((n, n, nmat)) + 1j * rng.standard_normal((n, n, nmat))
+    bad = m.copy()
+    bad[:, 2, 1] = 0.0
+    a = _to_device(bad, torch)
+    out = torch.empty_like(a)
+    stream = torch.cuda.current_stream().cuda_stream
+    assert L.rp_zinv_batched_noalloc(a.data_ptr(), out.data_ptr(), n, nmat, stream) == 3
+    assert b"singular" in L.rp_last_error(None)
+    a = _to_device(m, torch)
+    assert L.rp_zinv_batched_noalloc(a.data_ptr(), out.data_ptr(), n, nmat, stream) == 0
+    got = _from_device(out, n, nmat)
+    for e in range(nmat):
+        np.testing.assert_allclose(got[:, :, e], np.linalg.inv(m[:, :, e]), rtol=0, atol=1e-12 * np.abs(
+            np.linalg.inv(m[:, :, e])).max())
+
+
+@pytest.mark.gpu
 def test_noalloc_matches_epsinv_q_two_calls(case_dir, fresh_copy):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
