@@ -141,6 +141,55 @@ int rp_transfer_bytes(const rp_ctx *ctx, long long *h2d, long long *d2h);
 const char *rp_last_error(const rp_ctx *ctx);
 void rp_ctx_destroy(rp_ctx *ctx);
 
+/* ---- calc_int: Wannier-basis interaction integrals --------------------------
+ * calc_w3d (bare Coulomb V, screened W: src/calc_int/calc_intW.F) and calc_j3d
+ * (bare exchange X, screened exchange J: src/calc_int/calc_intJ.F).  Inputs:
+ * dir-wfn, dir-wan/dat.wan and dat.wan-center (Wannier functions on the full
+ * k mesh), dir-eps from calc_chiqw (dat.chi_cutoff, dat.wgrid, qNNN/dat.sq and
+ * dat.epsqw.600-602). */
+
+/* &param_calc_int (src/calc_int/m_rdinput.f90:7-29) plus &param_gpu extensions. */
+typedef struct rp_int_params {
+  int    calc_ifreq;           /* 1-based frequency written to dat.Wmat / dat.Jmat */
+  int    ix_intj_min, ix_intj_max, iy_intj_min, iy_intj_max, iz_intj_min, iz_intj_max;
+  double wcut_mvmc, jcut_mvmc; /* eV */
+  /* --- &param_gpu extensions --- */
+  int    fft_box[3];           /* 0 0 0: reference rule (calc_intW.F:150-185) */
+  int    device;
+  int    write_files;          /* 1: write dir-intW / dir-intJ / dir-mvmc */
+} rp_int_params;
+
+void rp_int_default_params(rp_int_params *p);
+/* Replaces read_input of src/calc_int/m_rdinput.f90:15-35. */
+int rp_int_parse_namelist(const char *text, rp_int_params *p);
+
+typedef struct rp_int rp_int;
+
+/* Reads every input like calc_intW.F:1-630 (k and q unfolding, make_LG0,
+ * eps^-1 of the irreducible q as complex(4)) and computes the real-space
+ * Wannier functions on the device once. */
+int rp_int_create(rp_int **out, const char *root, const rp_int_params *p);
+/* nwf, ne, number of q points, and Na (the R box is -Na..Na, Na = nkb/2). */
+int rp_int_dims(const rp_int *c, int *nwf, int *ne, int *ntq, int *na3);
+
+/* calc_w3d: V (nwf, nwf, 2Na1+1, 2Na2+1, 2Na3+1) and W (..., ne), complex
+ * interleaved, column-major, R1 fastest (V_MAT / W_MAT of calc_intW.F:942-985,
+ * heads included).  Writes dir-intW and dir-mvmc when write_files.  V, W may
+ * be NULL. */
+int rp_int_w3d(rp_int *c, double *V, double *W);
+/* calc_j3d: X and J on the same box (zero outside the IX/IY/IZ range;
+ * calc_intJ.F:609-905).  Writes dir-intJ and dir-mvmc when write_files. */
+int rp_int_j3d(rp_int *c, double *X, double *J);
+/* Device seconds of the last rp_int_w3d / rp_int_j3d: [0] pair densities,
+ * [1] k sums, [2] eps^-1 products, [3] q -> R sums, [4] total. */
+int rp_int_stage_times(const rp_int *c, double *t5);
+const char *rp_int_last_error(const rp_int *c);
+void rp_int_destroy(rp_int *c);
+
+/* Whole programs (stdin namelist text of the reference) in directory root. */
+int rp_calc_w3d(const char *root, const char *namelist_text);
+int rp_calc_j3d(const char *root, const char *namelist_text);
+
 /* Batched inverse of nmat complex n x n matrices (column-major, interleaved
  * re/im doubles, matrix m at a + 2*m*n*n) that allocates no device memory.
  * No counterpart in the reference: it is the inversion step of rp_epsinv_q

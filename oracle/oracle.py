@@ -17,8 +17,8 @@ LIB = os.path.join(HERE, "librp_oracle.so")
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "rp_oracle.c")
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("rp_oracle.c", "rp_oracle_int.c", "rp_oracle.h")]
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(s) for s in srcs):
         subprocess.check_call(["make", "-s", "-C", HERE])
     return LIB
 
@@ -41,6 +41,18 @@ class Report(C.Structure):
     _fields_ = [("nq_done", C.c_int), ("ntk", C.c_int), ("ng_last", C.c_int), ("npair_last", C.c_int),
                 ("npair_full_last", C.c_int), ("nen", C.c_int), ("fft_box", C.c_int * 3),
                 ("seconds_total", C.c_double), ("seconds_last_q", C.c_double)]
+
+
+class IntParams(C.Structure):
+    _fields_ = [("calc_ifreq", C.c_int), ("ix_min", C.c_int), ("ix_max", C.c_int), ("iy_min", C.c_int),
+                ("iy_max", C.c_int), ("iz_min", C.c_int), ("iz_max", C.c_int), ("wcut_mvmc", C.c_double),
+                ("jcut_mvmc", C.c_double), ("fft_box", C.c_int * 3), ("nthreads", C.c_int),
+                ("write_files", C.c_int), ("do_w", C.c_int), ("do_j", C.c_int)]
+
+
+class IntDims(C.Structure):
+    _fields_ = [("nwf", C.c_int), ("ne", C.c_int), ("ntq", C.c_int), ("na", C.c_int * 3), ("nkb", C.c_int * 3),
+                ("box", C.c_int), ("fft_box", C.c_int * 3), ("seconds", C.c_double)]
 
 
 _lib: Optional[C.CDLL] = None
@@ -71,6 +83,9 @@ def lib() -> C.CDLL:
                                  C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p]
         L.orc_tt_one.restype = C.c_int
         L.orc_last_error.restype = C.c_char_p
+        L.orc_int_default_params.argtypes = [C.POINTER(IntParams)]
+        L.orc_calc_int.argtypes = [C.c_char_p, C.POINTER(IntParams), C.POINTER(IntDims)] + [C.c_void_p] * 4
+        L.orc_calc_int.restype = C.c_int
         _lib = L
     return _lib
 
@@ -159,3 +174,34 @@ def ttrhdrn_chi0(dmna, dmnr, nk, imt1, e1, e2, f1, f2, delt, dsgn, em, xo=None):
     if rc:
         raise RuntimeError(lib().orc_last_error().decode())
     return xo
+
+
+def make_int_params(**kw) -> IntParams:
+    p = IntParams()
+    lib().orc_int_default_params(C.byref(p))
+    box = kw.pop("fft_box", None)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    if box is not None:
+        p.fft_box[0], p.fft_box[1], p.fft_box[2] = box
+    return p
+
+
+def calc_int(root: str, params: IntParams):
+    """calc_w3d / calc_j3d restated: returns dims and V, W, X, J as complex arrays
+    shaped (nwf, nwf, 2Na1+1, 2Na2+1, 2Na3+1[, ne]) in Fortran order."""
+    dims = IntDims()
+    p0 = IntParams.from_buffer_copy(params)
+    p0.do_w = p0.do_j = p0.write_files = 0
+    if lib().orc_calc_int(root.encode(), C.byref(p0), C.byref(dims), None, None, None, None):
+        raise RuntimeError("oracle failed: " + lib().orc_last_error().decode())
+    shape = (dims.nwf, dims.nwf, 2 * dims.na[0] + 1, 2 * dims.na[1] + 1, 2 * dims.na[2] + 1)
+    out = {}
+    bufs = []
+    for name, extra in (("V", ()), ("W", (dims.ne,)), ("X", ()), ("J", (dims.ne,))):
+        a = np.zeros(shape + extra, dtype=np.complex128, order="F")
+        out[name] = a
+        bufs.append(a.ctypes.data)
+    if lib().orc_calc_int(root.encode(), C.byref(params), C.byref(dims), *bufs):
+        raise RuntimeError("oracle failed: " + lib().orc_last_error().decode())
+    return dims, out

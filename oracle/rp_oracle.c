@@ -1609,3 +1609,6 @@ int orc_calc_chiqw(const char *root, const orc_params *P, orc_report *rep) {
 }
 
 const char *orc_last_error(void) { return g_err; }
+
+/* calc_int (V, W, X, J): shares the readers, unfold, FFT and pair density above */
+#include "rp_oracle_int.c"

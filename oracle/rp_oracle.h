@@ -89,6 +89,31 @@ int  orc_tt_one(double dmna, double dmnr, const double *ee1, const double *ee2, 
 int  orc_ttrhdrn_simple(double dmna, double dmnr, int n1, int n2, int n3, const int *imt1,
                         const double *fk, const double *gk, double *xo);
 
+/* ---- calc_int: calc_w3d (V, W) and calc_j3d (X, J) ---- */
+/* &param_calc_int (src/calc_int/m_rdinput.f90:7-13) plus extensions */
+typedef struct orc_int_params {
+    int    calc_ifreq;                   /* 1-based frequency of dat.Wmat / dat.Jmat */
+    int    ix_min, ix_max, iy_min, iy_max, iz_min, iz_max;   /* IX_INTJ_MIN ... */
+    double wcut_mvmc, jcut_mvmc;         /* eV */
+    /* --- extensions --- */
+    int    fft_box[3];                   /* 0,0,0 = reference rule */
+    int    nthreads;
+    int    write_files;                  /* dir-intW / dir-intJ / dir-mvmc */
+    int    do_w, do_j;                   /* run calc_w3d / calc_j3d */
+} orc_int_params;
+
+typedef struct orc_int_dims {
+    int nwf, ne, ntq, na[3], nkb[3], box, fft_box[3];
+    double seconds;
+} orc_int_dims;
+
+void orc_int_default_params(orc_int_params *p);
+/* V (nwf, nwf, box) and W (nwf, nwf, box, ne), X and J likewise (zero outside
+ * the IX/IY/IZ range), complex interleaved, box = (2Na1+1)(2Na2+1)(2Na3+1)
+ * with R1 fastest; any pointer may be NULL. */
+int orc_calc_int(const char *root, const orc_int_params *p, orc_int_dims *dims, double *V, double *W,
+                 double *X, double *J);
+
 #ifdef __cplusplus
 }
 #endif

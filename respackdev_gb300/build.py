@@ -2,7 +2,7 @@
 
 Compiles every CUDA source for sm_103a (``-gencode arch=compute_103a,code=sm_103a``),
 the host C++ with g++, and links ``respackdev_gb300/lib/librespack_gb300.so`` plus
-the ``respackdev_gb300/bin/rp_calc_chiqw`` executable.  Objects go to
+the ``respackdev_gb300/bin/rp_calc_chiqw``, ``rp_calc_w3d`` and ``rp_calc_j3d`` executables.  Objects go to
 ``respackdev_gb300/_build``.  Compilation runs in parallel; a file is rebuilt when
 it or any header is newer than its object.
 """
@@ -22,6 +22,8 @@ LIBDIR = os.path.join(HERE, "lib")
 BINDIR = os.path.join(HERE, "bin")
 LIB = os.path.join(LIBDIR, "librespack_gb300.so")
 EXE = os.path.join(BINDIR, "rp_calc_chiqw")
+# executables: main source -> program (drop-ins for calc_chiqw, calc_w3d, calc_j3d)
+MAINS = {"rp_main.cpp": "rp_calc_chiqw", "rp_main_w3d.cpp": "rp_calc_w3d", "rp_main_j3d.cpp": "rp_calc_j3d"}
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
@@ -59,7 +61,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BINDIR, exist_ok=True)
     hdr = _newest_header()
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    lib_srcs = [s for s in srcs if not s.endswith("rp_main.cpp")]
+    lib_srcs = [s for s in srcs if os.path.basename(s) not in MAINS]
     jobs = []
     for s in srcs:
         o = os.path.join(BUILD, os.path.basename(s) + ".o")
@@ -78,13 +80,15 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
-    main_o = os.path.join(BUILD, "rp_main.cpp.o")
-    if force or not os.path.exists(EXE) or os.path.getmtime(EXE) < max(os.path.getmtime(LIB), os.path.getmtime(main_o)):
-        cmd = ["g++", "-o", EXE, main_o, f"-L{LIBDIR}", "-lrespack_gb300", "-Wl,-rpath,$ORIGIN/../lib",
-               f"-L{CUDA_HOME}/lib64", "-lcudart"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link of rp_calc_chiqw failed\n{r.stderr}")
+    for src, prog in MAINS.items():
+        main_o = os.path.join(BUILD, src + ".o")
+        exe = os.path.join(BINDIR, prog)
+        if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(LIB), os.path.getmtime(main_o)):
+            cmd = ["g++", "-o", exe, main_o, f"-L{LIBDIR}", "-lrespack_gb300", "-Wl,-rpath,$ORIGIN/../lib",
+                   f"-L{CUDA_HOME}/lib64", "-lcudart"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"link of {prog} failed\n{r.stderr}")
     return LIB
 
 

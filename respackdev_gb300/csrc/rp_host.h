@@ -62,6 +62,7 @@ void write_unformatted_record(const std::string &path, const void *buf, size_t n
 // ---- namelist (&param_chiqw, &param_gpu) -----------------------------------
 void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int> *qlist,
                          std::vector<double> *explicit_em);
+void parse_calc_int_namelist(const std::string &text, rp_int_params *p);
 
 // ---- the host model of one run ----------------------------------------------
 struct Setup {

@@ -322,6 +322,43 @@ extern "C" void rp_default_params(rp_params *p) {
   p->qshard_count = 1;
 }
 
+namespace rp {
+
+// &param_calc_int (src/calc_int/m_rdinput.f90:7-29) and the &param_gpu keys that apply
+void parse_calc_int_namelist(const std::string &text, rp_int_params *p) {
+  NlGroup g;
+  if (!find_group(text, "param_calc_int", g)) fail(1, "namelist &param_calc_int not found");
+  for (auto &kv : g.items) {
+    const std::string &k = kv.first;
+    const auto &v = kv.second;
+    if (k == "calc_ifreq") p->calc_ifreq = nl_int(v, k);
+    else if (k == "ix_intj_min") p->ix_intj_min = nl_int(v, k);
+    else if (k == "ix_intj_max") p->ix_intj_max = nl_int(v, k);
+    else if (k == "iy_intj_min") p->iy_intj_min = nl_int(v, k);
+    else if (k == "iy_intj_max") p->iy_intj_max = nl_int(v, k);
+    else if (k == "iz_intj_min") p->iz_intj_min = nl_int(v, k);
+    else if (k == "iz_intj_max") p->iz_intj_max = nl_int(v, k);
+    else if (k == "wcut_mvmc") p->wcut_mvmc = nl_real(v, k);
+    else if (k == "jcut_mvmc") p->jcut_mvmc = nl_real(v, k);
+    else fail(1, "namelist &param_calc_int: unknown name '%s'", k.c_str());
+  }
+  NlGroup gg;
+  if (find_group(text, "param_gpu", gg)) {
+    for (auto &kv : gg.items) {
+      const std::string &k = kv.first;
+      const auto &v = kv.second;
+      if (k == "fft_box") {
+        if (v.size() != 3) fail(1, "&param_gpu fft_box needs 3 integers");
+        for (int i = 0; i < 3; i++) p->fft_box[i] = (int)llround(to_num(v[i]));
+      } else if (k == "device") p->device = nl_int(v, k);
+      else if (k == "write_files") p->write_files = nl_int(v, k);
+      else fail(1, "namelist &param_gpu: unknown name '%s' for calc_int", k.c_str());
+    }
+  }
+}
+
+}  // namespace rp
+
 static thread_local std::string g_parse_err;
 
 extern "C" int rp_parse_namelist(const char *text, rp_params *p, int *qlist, int qcap, int *nq, double *em,

@@ -277,6 +277,51 @@ def write_dir_wfn(root: str, d: SynthData, ncomp: int = 1):
                 write_unformatted_record(f, np.ascontiguousarray(c[:, ib]).astype("<c16").tobytes())
 
 
+def _kcheck(k: np.ndarray, trs: bool):
+    """kcheck / kcheck_trs (chiqw_sub.F:668-771): fold a rotated k into the
+    first zone; returns the folded k and the integer shift RW."""
+    k = k.copy()
+    RW = np.zeros(3, dtype=np.int64)
+    for i in range(3):
+        if not trs:
+            d = 1.0e-6
+            if k[i] > 1.5 + d: k[i] -= 2.0; RW[i] = -2
+            if k[i] > 0.5 + d: k[i] -= 1.0; RW[i] = -1
+            if k[i] <= -1.5 + d: k[i] += 2.0; RW[i] = 2
+            if k[i] <= -0.5 + d: k[i] += 1.0; RW[i] = 1
+        else:
+            d = -1.0e-6
+            if k[i] >= 1.5 + d: k[i] -= 2.0; RW[i] = -2
+            if k[i] >= 0.5 + d: k[i] -= 1.0; RW[i] = -1
+            if k[i] < -1.5 + d: k[i] += 2.0; RW[i] = 2
+            if k[i] < -0.5 + d: k[i] += 1.0; RW[i] = 1
+    return k, RW
+
+
+def unfold_full_mesh(d: SynthData):
+    """Full k mesh in the reference's order (chiqw.F:437-480, calc_intW.F:210-272:
+    per irreducible k the symmetry image, then its time-reversed image, each kept
+    when new) with its plane-wave lists (make_KG0 at R k + RW, negated for the
+    time-reversed images).  The synthetic inputs carry only the identity, so
+    R = 1.  Returns (SK0 (ntk, 3), list of (ng, 3) int arrays)."""
+    ecut = 0.0
+    for ik in range(d.kpts.shape[0]):
+        kG = (d.kg[ik] + d.kpts[ik][None, :]) @ d.bvec
+        ecut = max(ecut, float(np.einsum("ij,ij->i", kG, kG).max()))
+    ecut += 1.0e-8
+    sk0, kgs = [], []
+    for ik in range(d.kpts.shape[0]):
+        for trs in (False, True):
+            kt, RW = _kcheck(d.kpts[ik].astype(np.float64), trs)
+            cand = -kt if trs else kt
+            if any(np.all(np.abs(x - cand) < 1.0e-4) for x in sk0):
+                continue
+            G = sphere(d.bvec, ecut, d.kpts[ik] + RW)
+            sk0.append(cand)
+            kgs.append(-G if trs else G)
+    return np.array(sk0), kgs
+
+
 def write_dir_wan(root: str, spec: SynthSpec, d: SynthData, full_kg: Optional[List[np.ndarray]] = None,
                   full_k: Optional[np.ndarray] = None):
     """Band-cRPA target window (dat.ns-nb, dat.umat) and, when ``spec.nwf`` is
@@ -304,7 +349,8 @@ def write_dir_wan(root: str, spec: SynthSpec, d: SynthData, full_kg: Optional[Li
                 f.write(" ".join("(%s,%s)" % (fmt_real(U[ib, jw].real).strip(), fmt_real(U[ib, jw].imag).strip())
                                  for jw in range(nwin)) + "\n")
     if spec.nwf > 0:
-        assert full_kg is not None and full_k is not None
+        if full_kg is None or full_k is None:
+            full_k, full_kg = unfold_full_mesh(d)
         centers = rng.uniform(0.0, 1.0, size=(spec.nwf, 3)) @ d.avec
         with open(os.path.join(w, "dat.wan-center"), "w") as f:
             f.write("#Wannier center\n#1:x, 2:y, 3:z (in xyz coord)\n")
@@ -344,6 +390,11 @@ CASES = {
     # odd mesh exercises the odd branch of make_index_kpt
     "tiny_odd": SynthSpec(nk=(3, 3, 3), nbands=10, nocc=4, ecut_psi=6.0, seed=13,
                           wan_lo=5, wan_hi=6),
+    # Wannier orbitals for calc_int (V, W, X, J) on the tiny and odd meshes
+    "tiny_wan": SynthSpec(nk=(2, 2, 2), nbands=12, nocc=4, ecut_psi=8.0, seed=21,
+                          wan_lo=5, wan_hi=7, nwf=3, wan_sigma=1.2),
+    "odd_wan": SynthSpec(nk=(3, 3, 3), nbands=10, nocc=4, ecut_psi=6.0, seed=23,
+                         wan_lo=5, wan_hi=6, nwf=2, wan_sigma=1.0),
     # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
     "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
 }

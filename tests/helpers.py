@@ -65,3 +65,24 @@ def namelist_text(kw: dict, em=None, extra_gpu: str = "") -> str:
     if gpu:
         lines.append("&param_gpu " + ", ".join(gpu) + " /")
     return "\n".join(lines) + "\n"
+
+
+# frequencies of the calc_int cases (Hartree): static, one real, one imaginary
+EM_INT = np.array([0.0, 2.0 / AU, 3.0j / AU], dtype=np.complex128)
+
+
+def read_int_matrix(path: str, nwf: int):
+    """dat.Vmat / dat.Wmat / dat.Xmat / dat.Jmat -> {(R1, R2, R3): (nwf, nwf) complex in eV}."""
+    out = {}
+    with open(path) as f:
+        lines = [ln for ln in f.read().splitlines() if ln.strip() and not ln.startswith("#")]
+    i = 0
+    while i < len(lines):
+        R = tuple(int(x) for x in lines[i].split())
+        M = np.zeros((nwf, nwf), dtype=np.complex128)
+        for t in range(nwf * nwf):
+            a, b, re, im = lines[i + 1 + t].split()
+            M[int(a) - 1, int(b) - 1] = float(re) + 1j * float(im)
+        out[R] = M
+        i += 1 + nwf * nwf
+    return out

@@ -1,0 +1,75 @@
+"""calc_int on the GPU (rp_int_* of the C ABI) against the oracle: V, W of
+calc_w3d and X, J of calc_j3d, the executables and their files."""
+from __future__ import annotations
+
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from respackdev_gb300 import build as rp_build
+from respackdev_gb300 import calc_int as ci
+from tests.helpers import read_int_matrix
+
+pytestmark = pytest.mark.gpu
+
+# V, W, X, J relative to their largest element: the pair densities are rounded
+# to single precision like the reference, everything after them is FP64
+TOL = 1e-6
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("case,jr", [("tiny_wan", (0, 0)), ("tiny_wan", (-1, 1)), ("odd_wan", (-1, 1))])
+def test_vwxj_match_oracle(case, jr, int_case, int_copy):
+    src = int_case(case)
+    root = int_copy(src)
+    dims, ref = orc.calc_int(root, orc.make_int_params(nthreads=4, ix_min=jr[0], ix_max=jr[1], write_files=0))
+    p = ci.default_params(ix_intj_min=jr[0], ix_intj_max=jr[1], write_files=0)
+    with ci.IntContext(root, p) as c:
+        assert (c.nwf, c.ne, c.na) == (dims.nwf, dims.ne, tuple(dims.na))
+        V, W = c.w3d()
+        X, J = c.j3d()
+        t = c.stage_times()
+    for name, got in (("V", V), ("W", W), ("X", X), ("J", J)):
+        err = _rel(got, ref[name])
+        assert err < TOL, f"{case} {name}: {err:.3e}"
+    assert t[4] > 0
+
+
+def test_executables_write_the_files(int_case, int_copy):
+    rp_build.build()
+    root = int_copy(int_case("tiny_wan"))
+    nl = "&param_calc_int\n calc_ifreq=2, ix_intJ_min=0, ix_intJ_max=1, wcut_mvmc=0.5, jcut_mvmc=0.01 /\n"
+    for prog in ("rp_calc_w3d", "rp_calc_j3d"):
+        r = subprocess.run([os.path.join(rp_build.BINDIR, prog)], input=nl, text=True,
+                           cwd=root, capture_output=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+    dims, ref = orc.calc_int(root, orc.make_int_params(nthreads=4, ix_min=0, ix_max=1, calc_ifreq=2, write_files=0))
+    na = tuple(dims.na)
+    AU = 27.21151
+    Vf = read_int_matrix(os.path.join(root, "dir-intW", "dat.Vmat"), dims.nwf)
+    Jf = read_int_matrix(os.path.join(root, "dir-intJ", "dat.Jmat"), dims.nwf)
+    scale = np.abs(ref["V"]).max() * AU
+    for R, M in Vf.items():
+        idx = tuple(r + n for r, n in zip(R, na))
+        assert np.abs(M - ref["V"][(slice(None), slice(None)) + idx] * AU).max() < TOL * scale + 1e-9
+    for R, M in Jf.items():
+        idx = tuple(r + n for r, n in zip(R, na))
+        assert np.abs(M - ref["J"][(slice(None), slice(None)) + idx + (1,)] * AU).max() < TOL * scale + 1e-9
+    for f in ("zCoulombIntra.def", "zCoulombInter.def", "zHund.def", "zExchange.def", "zPairHop.def"):
+        assert os.path.exists(os.path.join(root, "dir-mvmc", f))
+    for f in ("dat.Wmat", "dat.VvsR.001", "dat.WvsR.003", "dat.UvsE.001-003"):
+        assert os.path.exists(os.path.join(root, "dir-intW", f))
+
+
+def test_bad_range_is_an_input_error(int_case, int_copy):
+    root = int_copy(int_case("tiny_wan"))
+    p = ci.default_params(ix_intj_min=-3, ix_intj_max=3, write_files=0)
+    with ci.IntContext(root, p) as c:
+        with pytest.raises(RuntimeError, match="intJ range"):
+            c.j3d()
