@@ -194,6 +194,12 @@ def run_reference(args):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def shard_q(nq_all: int, rank: int, world: int):
+    """q points of one rank: every world-th point after Gamma (weak scaling;
+    the reference's MPI_num_qcomm q communities, chiqw.F:662-687)."""
+    return list(range(2, nq_all + 1))[rank::world]
+
+
 def normwise(a, b):
     w = 0.0
     for i in range(b.shape[2]):
@@ -226,8 +232,7 @@ def run_gpu(args):
         info = ctx.info()
         nq_all = ctx.L.rp_num_qirr(ctx._h)
         # q points of this rank (weak scaling: every rank takes its own q points), Gamma excluded
-        qs = [iq for iq in range(2, nq_all + 1)]
-        mine = qs[rank::world]
+        mine = shard_q(nq_all, rank, world)
         need = args.warmup + args.steps
         mine = (mine * (need // max(1, len(mine)) + 1))[:need]
         for iq in mine[: args.warmup]:

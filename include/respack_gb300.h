@@ -122,8 +122,17 @@ int rp_epsinv_q(rp_ctx *ctx, double *epsinv);
 int rp_write_q(rp_ctx *ctx, const char *root);
 
 /* Whole calc_chiqw run (PROGRAM DIELECTRIC, chiqw.F:1-2100) in directory
- * root with the namelist text (stdin content of the reference). */
+ * root with the namelist text (stdin content of the reference).  With
+ * &param_gpu qshard_index/qshard_count, one process per GPU takes every
+ * qshard_count-th q point still to do (the reference's MPI_num_qcomm
+ * q communities, chiqw.F:662-687); no data is exchanged. */
 int rp_calc_chiqw(const char *root, const char *namelist_text);
+
+/* The 1-based q points rp_calc_chiqw would compute in root with this namelist
+ * (host only, no device): the q list or every q without dat.log.400
+ * (chiqw.F:593-608), then this process's shard.  Fills up to cap entries and
+ * the count *n. */
+int rp_plan_q(const char *root, const char *namelist_text, int *qlist, int cap, int *n);
 
 /* Seconds spent in each stage of the last rp_chi0_q + rp_epsinv_q (device
  * time from CUDA events): [0] tetrahedron weights, [1] pair densities,

@@ -221,3 +221,18 @@ def calc_chiqw(root: str, namelist_text: str) -> None:
     rc = L.rp_calc_chiqw(root.encode(), namelist_text.encode())
     if rc:
         raise RuntimeError(f"rp_calc_chiqw failed ({rc}): {L.rp_last_error(None).decode()}")
+
+
+def plan_q(root: str, namelist_text: str) -> list:
+    """1-based q points a calc_chiqw run with this namelist would compute in
+    ``root`` (its &param_gpu q shard included).  Host only: needs no GPU."""
+    L = load()
+    L.rp_plan_q.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int)]
+    L.rp_plan_q.restype = C.c_int
+    cap = 4096
+    buf = (C.c_int * cap)()
+    n = C.c_int(0)
+    rc = L.rp_plan_q(root.encode(), namelist_text.encode(), buf, cap, C.byref(n))
+    if rc:
+        raise RuntimeError(f"rp_plan_q failed ({rc}): {L.rp_last_error(None).decode()}")
+    return list(buf[: min(n.value, cap)])

@@ -556,6 +556,48 @@ const char *rp_last_error(const rp_ctx *c) { return c ? c->err.c_str() : g_creat
 
 void rp_ctx_destroy(rp_ctx *c) { delete c; }
 
+// q points (0-based) that a calc_chiqw run with parameters p computes in root:
+// the manual list or every q without dat.log (chiqw.F:593-608), then this
+// process's shard of them (qshard_index of qshard_count, taken modulo).
+static std::vector<int> plan_q(const rp::Setup &S, const rp_params &p, const std::vector<int> &qlist,
+                               const std::string &root) {
+  const std::string epsdir = root + "/dir-eps";
+  char buf[64];
+  std::vector<int> todo;
+  if (p.flg_calc_type == 2) {
+    struct stat stt;
+    for (int ik : qlist) {
+      if (ik < 1 || ik > S.nk_irr) rp::fail(1, "q index %d outside dat.sample-k", ik);
+      snprintf(buf, sizeof buf, "/q%03d/dat.log.%03d", ik, p.file_num_log_start);
+      if (stat((epsdir + buf).c_str(), &stt) != 0) todo.push_back(ik - 1);
+    }
+  } else {
+    todo = rp::q_list(S, epsdir);
+  }
+  const int ns = std::max(1, p.qshard_count), si = p.qshard_index;
+  if (si < 0 || si >= ns) rp::fail(1, "qshard_index %d outside 0..%d", si, ns - 1);
+  std::vector<int> mine;
+  for (size_t i = 0; i < todo.size(); i++)
+    if ((int)(i % ns) == si) mine.push_back(todo[i]);
+  return mine;
+}
+
+int rp_plan_q(const char *root, const char *namelist_text, int *qlist, int cap, int *n) {
+  return guarded(nullptr, [&] {
+    rp_params p;
+    rp_default_params(&p);
+    std::vector<int> ql;
+    std::vector<double> em;
+    rp::parse_namelist_text(namelist_text ? namelist_text : "", &p, &ql, &em);
+    rp::Setup S;
+    S.params = p;
+    rp::read_dir_wfn(S, root);
+    const std::vector<int> mine = plan_q(S, p, ql, root);
+    if (n) *n = (int)mine.size();
+    for (int i = 0; i < (int)mine.size() && i < cap && qlist; i++) qlist[i] = mine[i] + 1;
+  });
+}
+
 int rp_calc_chiqw(const char *root, const char *namelist_text) {
   rp_params p;
   rp_default_params(&p);
@@ -572,17 +614,7 @@ int rp_calc_chiqw(const char *root, const char *namelist_text) {
     mkdir_p(epsdir);
     char buf[64];
     for (int ik = 0; ik < S.nk_irr; ik++) { snprintf(buf, sizeof buf, "/q%03d", ik + 1); mkdir_p(epsdir + buf); }
-    std::vector<int> todo;
-    if (p.flg_calc_type == 2) {
-      struct stat stt;
-      for (int ik : qlist) {
-        if (ik < 1 || ik > S.nk_irr) rp::fail(1, "q index %d outside dat.sample-k", ik);
-        snprintf(buf, sizeof buf, "/q%03d/dat.log.%03d", ik, p.file_num_log_start);
-        if (stat((epsdir + buf).c_str(), &stt) != 0) todo.push_back(ik - 1);
-      }
-    } else {
-      todo = rp::q_list(S, epsdir);
-    }
+    const std::vector<int> mine = plan_q(S, p, qlist, root);
     // shared files (chiqw.F:1206-1215)
     FILE *f = fopen((epsdir + "/dat.chi_cutoff").c_str(), "w");
     if (f) { fprintf(f, " %24.16E\n", S.ecut_eps); fclose(f); }
@@ -592,10 +624,8 @@ int rp_calc_chiqw(const char *root, const char *namelist_text) {
       for (auto &e : S.em) fprintf(f, "%15.10f%15.10f\n", e.real(), e.imag());
       fclose(f);
     }
-    const int ns = std::max(1, p.qshard_count), si = p.qshard_index;
-    for (size_t i = 0; i < todo.size(); i++) {
-      if ((int)(i % ns) != si) continue;
-      chi0_q(c, todo[i] + 1, p.precision != RP_PREC_FP64);
+    for (int iq : mine) {
+      chi0_q(c, iq + 1, p.precision != RP_PREC_FP64);
       epsinv_run(c);
       write_q(c, root);
     }
