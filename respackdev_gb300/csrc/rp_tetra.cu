@@ -272,56 +272,245 @@ __device__ bool tetra_terms(double dmna, double dmnr, const cx *ffk, const cx *g
   return true;
 }
 
-// Normal case (no near-degenerate vertices) of calc() with shared vertex logs.
-// All four g share the imaginary part delt*dsgn, so d_ab = g_a - g_b is real and
-// log(z_a / z_b) = L_a - L_b with L = log(g + w) (z_a, z_b in the same half
-// plane).  The closed forms of sub2normal / sub1normal (:346-363, :435-451) then
-// need only real reciprocal differences, shared across frequencies.
+// Normal case of calc() (chk1 finds no near-degenerate pair, so ia4 holds the
+// positions 1, 2, 3, 0: m_tetrahedron_20170325.F:457-503, calc :209-235) with
+// shared vertex logs.  All four g share the imaginary part delt*dsgn, so
+// g_a - g_b is real and log(z_a / z_b) = L_a - L_b with L = log(g + w) (z_a,
+// z_b in the same half plane).  The closed forms sub2normal / sub1normal
+// (:346-363, :435-451) then need only real reciprocal differences
+// id(a,b) = 1/(gr_a - gr_b), computed once per tetrahedron for every frequency
+// and both signs: the sign -1 negates every gr, which flips the coefficients
+// of odd degree in id and leaves the others.  Every vertex index below is a
+// compile-time constant, so all per-vertex values stay in registers.
 struct NormalCoef {
-  double A[3], B[3], C[3], D[3];   // the three sub2normal forms
-  double S1a, S1b, S1c;            // sub1normal
-  int p[3], q[3], r[3], s[3];
-  int a0, a1, a2, a3;
+  double A[3], B[3], C[3], D[3];   // sub2normal forms c1, c2, c3
+  double S1a, S1b, S1c;            // sub1normal form c4
 };
 
-__device__ __forceinline__ void normal_coef(const double *gr, const int *a, NormalCoef &c) {
-  double id[4][4];
-  for (int i = 0; i < 4; i++)
-    for (int j = 0; j < 4; j++) id[i][j] = (i == j) ? 0.0 : 1.0 / (gr[i] - gr[j]);
-  c.a0 = a[0]; c.a1 = a[1]; c.a2 = a[2]; c.a3 = a[3];
-  // c1 = sub2normal(g[a1], g[a0], g[a2], g[a3]), c2 = sub2normal(a0, a1, a2, a3), c3 = sub2normal(a0, a2, a1, a3)
-  const int P[3] = {a[1], a[0], a[0]}, Q[3] = {a[0], a[1], a[2]}, R[3] = {a[2], a[2], a[1]}, S[3] = {a[3], a[3], a[3]};
-  for (int f = 0; f < 3; f++) {
-    const int p = P[f], q = Q[f], r = R[f], s = S[f];
-    c.p[f] = p; c.q[f] = q; c.r[f] = r; c.s[f] = s;
-    c.A[f] = id[p][q] * id[q][r] * id[q][s] / 6.0;
-    c.B[f] = id[p][r] * id[q][r] * id[q][r] * id[r][s] / 6.0;
-    c.C[f] = id[p][s] * id[q][s] * id[q][s] * id[r][s] / 6.0;
-    c.D[f] = id[p][q] * id[p][q] * id[p][r] * id[p][s] / 6.0;
-  }
-  // c4 = sub1normal(g0 = a0, g1 = a3, g2 = a1, g3 = a2)
-  const int p = a[0], q = a[3], r = a[1], s = a[2];
-  c.S1a = 0.5 * id[p][r] * id[p][s] * id[p][q];
-  c.S1b = 0.5 * id[p][r] * id[q][r] * id[r][s];
-  c.S1c = 0.5 * id[q][s] * id[p][s] * id[r][s];
+// id(i,j) from r = {id01, id02, id03, id12, id13, id23}; i, j constants after inlining
+__device__ __forceinline__ double idr(const double (&r)[6], int i, int j) {
+  const bool neg = i > j;
+  const int a = neg ? j : i, b = neg ? i : j;
+  const int k = a == 0 ? b - 1 : (a == 1 ? b + 1 : 5);
+  return neg ? -r[k] : r[k];
 }
 
-// vertex terms for one frequency given z_a = g_a + w, z^2, z^3 and L_a = log z_a
-__device__ __forceinline__ void normal_terms(const NormalCoef &c, const cx *z2, const cx *z3, const cx *L,
-                                             const cx *fk, cx *x) {
-  cx F[3];
-  for (int f = 0; f < 3; f++) {
-    const int p = c.p[f], q = c.q[f], r = c.r[f], s = c.s[f];
-    F[f] = -(z2[q] * c.A[f]) - z3[r] * (L[r] - L[q]) * c.B[f] + z3[s] * (L[s] - L[q]) * c.C[f] +
-           z3[p] * (L[p] - L[q]) * c.D[f];
+template <int P, int Q, int R, int S>
+__device__ __forceinline__ void coef2(const double (&r)[6], double &A, double &B, double &C, double &D) {
+  A = idr(r, P, Q) * idr(r, Q, R) * idr(r, Q, S) / 6.0;
+  B = idr(r, P, R) * idr(r, Q, R) * idr(r, Q, R) * idr(r, R, S) / 6.0;
+  C = idr(r, P, S) * idr(r, Q, S) * idr(r, Q, S) * idr(r, R, S) / 6.0;
+  D = idr(r, P, Q) * idr(r, P, Q) * idr(r, P, R) * idr(r, P, S) / 6.0;
+}
+
+// sign +1 coefficients: c1 = sub2normal(g2, g1, g3, g0), c2 = sub2normal(g1, g2, g3, g0),
+// c3 = sub2normal(g1, g3, g2, g0), c4 = sub1normal(g1, g0, g2, g3)
+__device__ __forceinline__ void normal_coef(const double (&gr)[4], NormalCoef &c) {
+  const double d01 = gr[0] - gr[1], d02 = gr[0] - gr[2], d03 = gr[0] - gr[3];
+  const double d12 = gr[1] - gr[2], d13 = gr[1] - gr[3], d23 = gr[2] - gr[3];
+  const double r[6] = {1.0 / d01, 1.0 / d02, 1.0 / d03, 1.0 / d12, 1.0 / d13, 1.0 / d23};
+  coef2<2, 1, 3, 0>(r, c.A[0], c.B[0], c.C[0], c.D[0]);
+  coef2<1, 2, 3, 0>(r, c.A[1], c.B[1], c.C[1], c.D[1]);
+  coef2<1, 3, 2, 0>(r, c.A[2], c.B[2], c.C[2], c.D[2]);
+  c.S1a = 0.5 * idr(r, 1, 2) * idr(r, 1, 3) * idr(r, 1, 0);
+  c.S1b = 0.5 * idr(r, 1, 2) * idr(r, 0, 2) * idr(r, 2, 3);
+  c.S1c = 0.5 * idr(r, 0, 3) * idr(r, 1, 3) * idr(r, 2, 3);
+}
+
+template <int P, int Q, int R, int S>
+__device__ __forceinline__ cx s2term(const cx (&z2)[4], const cx (&z3)[4], const cx (&L)[4], double A, double B,
+                                     double C, double D) {
+  return -(z2[Q] * A) - z3[R] * (L[R] - L[Q]) * B + z3[S] * (L[S] - L[Q]) * C + z3[P] * (L[P] - L[Q]) * D;
+}
+
+// vertex terms x (positions 0..3) of one sign: z_a = g_a + w, L_a = log z_a; sg = +1 or -1
+__device__ __forceinline__ void normal_terms(const NormalCoef &c, double sg, const cx (&z)[4], const cx (&L)[4],
+                                             cx (&x)[4]) {
+  cx z2[4], z3[4];
+#pragma unroll
+  for (int v = 0; v < 4; v++) { z2[v] = z[v] * z[v]; z3[v] = z2[v] * z[v]; }
+  const cx F0 = s2term<2, 1, 3, 0>(z2, z3, L, c.A[0] * sg, c.B[0], c.C[0], c.D[0]);
+  const cx F1 = s2term<1, 2, 3, 0>(z2, z3, L, c.A[1] * sg, c.B[1], c.C[1], c.D[1]);
+  const cx F2 = s2term<1, 3, 2, 0>(z2, z3, L, c.A[2] * sg, c.B[2], c.C[2], c.D[2]);
+  // sub1normal(g1, g0, g2, g3): p = 1, q = 0, r = 2, s = 3
+  const cx lq = z2[0] * (L[0] - L[1]), lr = z2[2] * (L[2] - L[1]), ls = z2[3] * (L[3] - L[1]);
+  const cx F4 = -(lq * (c.S1a * sg)) - (lq - lr) * (c.S1b * sg) + (lq - ls) * (c.S1c * sg);
+  // fk = dsgn on every vertex
+  x[1] = F0 * sg;
+  x[2] = F1 * sg;
+  x[3] = F2 * sg;
+  x[0] = (F4 - F2 - F1 - F0) * sg;
+}
+
+// Near-degenerate, uncut tetrahedra with shared logs.  The reference's special
+// forms (sub1g30g21 ... sub2simple, m_tetrahedron_20170325.F:304-451) are
+// evaluated at points that all share the imaginary part delt*dsgn -- the
+// vertices and the averages geq of the degenerate ones -- so every energy
+// difference is real and log(z_a / z_b) = L_a - L_b.  Vertex logs come from
+// the shared table; only the averages need a log of their own.
+struct Pt { double g; cx Z, L; };  // real part of g, z = g + w, log z
+
+__device__ __forceinline__ cx f_s1g30g21(const Pt &p0, const Pt &p1) {
+  const double d = p0.g - p1.g;
+  return (0.5 * (p0.Z + p1.Z)) / (d * d) - (p0.L - p1.L) * p0.Z * p1.Z / (d * d * d);
+}
+__device__ __forceinline__ cx f_s1g30g20(const Pt &p0, const Pt &p1) {
+  const double d = p0.g - p1.g;
+  return (p0.Z - 3.0 * p1.Z) * 0.25 / (d * d) + p1.Z * p1.Z * (p0.L - p1.L) * 0.5 / (d * d * d);
+}
+__device__ __forceinline__ cx f_s1g30(const Pt &p0, const Pt &p1, const Pt &p2) {
+  const double d02 = p0.g - p2.g, d01 = p0.g - p1.g, d12 = p1.g - p2.g, t = d02 * d01;
+  cx v = cx(0.5 / d02, 0.0);
+  v = v - 0.5 / (t * t) * p0.Z * (-2.0 * p1.Z * p2.Z + p0.Z * (p1.Z + p2.Z)) * (p0.L - p1.L);
+  v = v + 0.5 / (d02 * d02) * p2.Z * p2.Z * (p1.L - p2.L) / d12;
+  return v + 0.5 / (d02 * d01) * p1.Z;
+}
+__device__ __forceinline__ cx f_s2g30g20(const Pt &p0, const Pt &p1) {
+  const double d = p0.g - p1.g;
+  return (d * (p0.Z + 2.0 * p1.Z) - 6.0 * p0.Z * p1.Z) / (12.0 * (d * d * d)) +
+         p0.Z * p1.Z * p1.Z * (p0.L - p1.L) / (d * d * d * d) * 0.5;
+}
+__device__ __forceinline__ cx f_s2g30g10(const Pt &p0, const Pt &p2) {
+  const double d = p0.g - p2.g;
+  return (2.0 * p0.Z * p0.Z - 7.0 * p0.Z * p2.Z + 11.0 * p2.Z * p2.Z) / (36.0 * (d * d * d)) -
+         p2.Z * p2.Z * p2.Z * (p0.L - p2.L) / (6.0 * (d * d * d * d));
+}
+__device__ __forceinline__ cx f_s2g10(const Pt &p0, const Pt &p2, const Pt &p3) {
+  const double d2 = p0.g - p2.g, d3 = p0.g - p3.g, d23 = p2.g - p3.g;
+  cx v = p0.Z * (p0.Z * p0.Z + 5.0 * p2.Z * p3.Z - 3.0 * p0.Z * (p2.Z + p3.Z)) / (12.0 * (d2 * d2) * (d3 * d3));
+  v = v - p2.Z * p2.Z * p2.Z * (p2.L - p0.L) / (6.0 * (d2 * d2 * d2) * d23);
+  return v + p3.Z * p3.Z * p3.Z * (p3.L - p0.L) / (6.0 * (d3 * d3 * d3) * d23);
+}
+__device__ __forceinline__ cx f_s2g30(const Pt &p0, const Pt &p1, const Pt &p2) {
+  const double d01 = p0.g - p1.g, d02 = p0.g - p2.g, d12 = p1.g - p2.g;
+  cx v = (p0.Z * p0.Z * d12 + p1.Z * p1.Z * d02) / (6.0 * d02 * (d01 * d01) * d12);
+  v = v - p0.Z * p0.Z * (2.0 * p1.Z * d02 + p2.Z * d01) * (p0.L - p2.L) / (6.0 * (d02 * d02) * (d01 * d01 * d01));
+  return v + p1.Z * p1.Z * (2.0 * p0.Z * d12 - p2.Z * d01) * (p1.L - p2.L) / (6.0 * (d01 * d01 * d01) * (d12 * d12));
+}
+
+// point at the average of the vertices in idx[0..n) (calc :243-296)
+__device__ __forceinline__ Pt avg_pt(const double (&g)[4], const int *idx, int n, double dg, cx w) {
+  double s = g[idx[0]];
+  for (int i = 1; i < n; i++) s += g[idx[i]];
+  Pt p;
+  p.g = s / (double)n;
+  p.Z = cx(p.g + w.r, dg + w.i);
+  p.L = clog_(p.Z);
+  return p;
+}
+
+// vertex terms of calc() for chk1 cases 2, 3 and 4 (one frequency, one sign),
+// positions 0..3; fk = dsgn on every vertex.  Returns false on a bad case.
+__device__ __forceinline__ bool degen_terms(const Chk &c, const Pt (&v)[4], const double (&g)[4], double dg, cx w,
+                                            double dsgn, cx (&x)[4]) {
+  switch (c.s) {
+  case 2: {
+    const Pt q = avg_pt(g, c.ia3, 2, dg, w);
+    const cx c1 = f_s2g10(q, v[c.ia4[0]], v[c.ia4[1]]);
+    const cx c2 = f_s2g30(q, v[c.ia4[0]], v[c.ia4[1]]);
+    const cx c3 = f_s1g30(q, v[c.ia4[1]], v[c.ia4[0]]);
+    x[c.ia3[0]] = c1 * dsgn;
+    x[c.ia3[1]] = c1 * dsgn;
+    x[c.ia4[0]] = c2 * dsgn;
+    x[c.ia4[1]] = (c3 - c2 - c1 - c1) * dsgn;
+    return true;
   }
-  const int p = c.a0, q = c.a3, r = c.a1, s = c.a2;
-  const cx lq = z2[q] * (L[q] - L[p]), lr = z2[r] * (L[r] - L[p]), ls = z2[s] * (L[s] - L[p]);
-  const cx F4 = -(lq * c.S1a) - (lq - lr) * c.S1b + (lq - ls) * c.S1c;
-  x[c.a0] = fk[c.a0] * F[0];
-  x[c.a1] = fk[c.a1] * F[1];
-  x[c.a2] = fk[c.a2] * F[2];
-  x[c.a3] = fk[c.a3] * (F4 - F[2] - F[1] - F[0]);
+  case 3: {
+    const Pt q = avg_pt(g, c.ia3, 3, dg, w);
+    const cx c1 = f_s2g30g10(q, v[c.ia4[0]]);
+    const cx c2 = f_s1g30g20(q, v[c.ia4[0]]);
+    x[c.ia3[0]] = c1 * dsgn;
+    x[c.ia3[1]] = c1 * dsgn;
+    x[c.ia3[2]] = c1 * dsgn;
+    x[c.ia4[0]] = (c2 - c1 - c1 - c1) * dsgn;
+    return true;
+  }
+  case 4:
+    if (c.i3 == 2) {
+      const Pt q1 = avg_pt(g, c.ia3, 2, dg, w), q2 = avg_pt(g, c.ia3 + 2, 2, dg, w);
+      const cx c1 = f_s2g30g20(q1, q2);
+      const cx c2 = f_s1g30g21(q1, q2);
+      x[c.ia3[0]] = c1 * dsgn;
+      x[c.ia3[1]] = c1 * dsgn;
+      x[c.ia3[2]] = (c2 - c1 - c1) * 0.5 * dsgn;
+      x[c.ia3[3]] = (c2 - c1 - c1) * 0.5 * dsgn;
+      return true;
+    } else if (c.i3 >= 3 && c.i3 <= 6) {
+      const double s4 = (g[c.ia3[0]] + g[c.ia3[1]] + g[c.ia3[2]] + g[c.ia3[3]]) / 4.0;
+      const cx c1 = 1.0 / (cx(s4 + w.r, dg + w.i) * 24.0);
+      for (int a = 0; a < 4; a++) x[c.ia3[a]] = c1 * dsgn;
+      return true;
+    }
+    return false;
+  default:
+    return false;
+  }
+}
+
+// One (tetrahedron, sign) that is near-degenerate or cut by the Fermi level:
+// ttct and the reference's closed forms (m_tetrahedron_20170325.F:99-302).
+// Out of line, so that its large local arrays do not weigh on the normal path.
+__device__ __noinline__ void other_tetra(const TetraArgs &a, int code, const double *e1m, const double *e2m,
+                                         const double2 *Lt, int e0, int ne, int nec, double2 *xo) {
+  const double f = a.efermi, delt = a.delt;
+  const int t = code >> 1, sg = code & 1;
+  const double dsgn = sg == 0 ? 1.0 : -1.0;
+  int slot[4];
+  double ee1[4], ee2[4];
+  for (int v = 0; v < 4; v++) { slot[v] = a.imt1[4 * t + v]; ee1[v] = e1m[slot[v]]; ee2[v] = e2m[slot[v]]; }
+  const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
+  const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
+  if (mn2 > f && mx1 < f) {
+    cx ffk[4], ggk[4];
+    double g[4];
+    for (int v = 0; v < 4; v++) {
+      ffk[v] = cx(dsgn, 0);
+      ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
+      g[v] = ggk[v].r;
+    }
+    const Chk c = chk1(a.dmna, a.dmnr, ggk);
+    const double dg = delt * dsgn;
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      cx x[4];
+      bool ok;
+      if (dg + w.i == 0.0) {
+        // z on the real axis: the reference's ratio logs
+        ok = calc_w(c, ffk, ggk, w, x);
+      } else {
+        Pt p[4];
+        for (int v = 0; v < 4; v++) {
+          p[v].g = g[v];
+          p[v].Z = ggk[v] + w;
+          const double2 l = Lt[((size_t)sg * a.ntk + slot[v]) * nec + e];
+          p[v].L = cx(l.x, l.y);
+        }
+        ok = degen_terms(c, p, g, dg, w, dsgn, x);
+      }
+      if (!ok) { atomicExch(a.err, 2); continue; }
+      for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], x[v]);
+    }
+    return;
+  }
+  double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
+  for (int i = 0; i < 4; i++)
+    for (int v = 0; v < 4; v++) dwgt[0][i][v] = (i == v) ? 1.0 : 0.0;
+  dvol[0] = 1.0;
+  int nt = 1;
+  if (!ttct(f, ee2, +1, nt, dwgt, dvol) || !ttct(f, ee1, -1, nt, dwgt, dvol)) { atomicExch(a.err, 1); return; }
+  for (int i3 = 0; i3 < nt; i3++) {
+    cx ffk[4], ggk[4];
+    for (int i4 = 0; i4 < 4; i4++) {
+      double sm = 0;
+      for (int v = 0; v < 4; v++) sm += (ee2[v] - ee1[v]) * dwgt[i3][i4][v];
+      ffk[i4] = cx(dvol[i3], 0) * dsgn;
+      ggk[i4] = cx(-sm, delt) * dsgn;
+    }
+    double w4[4][4];
+    for (int i4 = 0; i4 < 4; i4++)
+      for (int v = 0; v < 4; v++) w4[i4][v] = dwgt[i3][i4][v];
+    if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, w4, xo)) atomicExch(a.err, 2);
+  }
 }
 
 // Tetrahedra are first sorted into shared-memory lists by the work they need --
@@ -356,7 +545,9 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
     const cx L = clog_(z);
     Lt[((size_t)sg * ntk + m) * nec + e] = make_double2(L.r, L.i);
   }
-  // classify (tetrahedron, sign): code = 2*t + sg
+  // classify: normal tetrahedra (both signs) from the front as t, the others
+  // from the back as 2*t + sign.  chk1 sees |g_a - g_b| and |g_a + g_b|, which
+  // the sign does not change, so one test covers both signs.
   for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
     double ee1[4], ee2[4];
     for (int v = 0; v < 4; v++) { const int sl = a.imt1[4 * t + v]; ee1[v] = e1m[sl]; ee2[v] = e2m[sl]; }
@@ -364,91 +555,69 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
     const double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
     const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
     if (mx2 <= f) continue;  // ttct(+1) drops the whole tetrahedron
-    const bool uncut = mn2 > f && mx1 < f;
-    for (int sg = 0; sg < 2; sg++) {
-      bool normal = false;
-      if (uncut) {
-        const double dsgn = sg == 0 ? 1.0 : -1.0;
-        cx ggk[4];
-        for (int v = 0; v < 4; v++) ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
-        normal = chk1(a.dmna, a.dmnr, ggk).s == 0;
-      }
-      if (normal) lists[atomicAdd(&n_normal, 1)] = 2 * t + sg;
-      else lists[2 * ntet - 1 - atomicAdd(&n_other, 1)] = 2 * t + sg;
+    bool normal = false;
+    if (mn2 > f && mx1 < f) {
+      cx ggk[4];
+      for (int v = 0; v < 4; v++) ggk[v] = cx(-(ee2[v] - ee1[v]), delt);
+      normal = chk1(a.dmna, a.dmnr, ggk).s == 0;
+    }
+    if (normal) {
+      lists[atomicAdd(&n_normal, 1)] = t;
+    } else {
+      const int o = atomicAdd(&n_other, 2);
+      lists[2 * ntet - 1 - o] = 2 * t;
+      lists[2 * ntet - 2 - o] = 2 * t + 1;
     }
   }
   __syncthreads();
-  // normal tetrahedra: shared logs, real reciprocal differences
+  // normal tetrahedra: shared logs, real reciprocal differences, both signs
   for (int idx = threadIdx.x; idx < n_normal; idx += blockDim.x) {
-    const int code = lists[idx], t = code >> 1, sg = code & 1;
-    const double dsgn = sg == 0 ? 1.0 : -1.0;
+    const int t = lists[idx];
     int slot[4];
-    cx ffk[4], ggk[4];
     double gr[4];
+#pragma unroll
     for (int v = 0; v < 4; v++) {
       slot[v] = a.imt1[4 * t + v];
-      ffk[v] = cx(dsgn, 0);
-      ggk[v] = cx(-(e2m[slot[v]] - e1m[slot[v]]), delt) * dsgn;
-      gr[v] = ggk[v].r;
+      gr[v] = -(e2m[slot[v]] - e1m[slot[v]]);
     }
-    const Chk c = chk1(a.dmna, a.dmnr, ggk);
     NormalCoef nc;
-    normal_coef(gr, c.ia4, nc);
+    normal_coef(gr, nc);
     for (int e = 0; e < ne; e++) {
       const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
-      cx x[4];
-      if (ggk[0].i + w.i == 0.0) {
-        // z on the real axis: keep the ratio logs of the reference
-        if (!calc_w(c, ffk, ggk, w, x)) { atomicExch(a.err, 2); continue; }
-      } else {
-        cx z2[4], z3[4], L[4];
-        for (int v = 0; v < 4; v++) {
-          const cx z = ggk[v] + w;
-          z2[v] = z * z;
-          z3[v] = z2[v] * z;
-          const double2 l = Lt[((size_t)sg * ntk + slot[v]) * nec + e];
-          L[v] = cx(l.x, l.y);
+      cx acc[4];
+#pragma unroll 1
+      for (int sg = 0; sg < 2; sg++) {
+        const double dsgn = sg == 0 ? 1.0 : -1.0;
+        cx x[4];
+        if (delt * dsgn + w.i == 0.0) {
+          // z on the real axis: keep the ratio logs of the reference
+          Chk c;
+          c.s = 0; c.i3 = 0;
+          c.ia4[0] = 1; c.ia4[1] = 2; c.ia4[2] = 3; c.ia4[3] = 0;
+          c.ia3[0] = c.ia3[1] = c.ia3[2] = c.ia3[3] = 0;
+          cx ffk[4], ggk[4];
+          for (int v = 0; v < 4; v++) { ffk[v] = cx(dsgn, 0); ggk[v] = cx(gr[v], delt) * dsgn; }
+          if (!calc_w(c, ffk, ggk, w, x)) { atomicExch(a.err, 2); x[0] = x[1] = x[2] = x[3] = cx(0, 0); }
+        } else {
+          cx z[4], L[4];
+#pragma unroll
+          for (int v = 0; v < 4; v++) {
+            z[v] = cx(gr[v] * dsgn + w.r, delt * dsgn + w.i);
+            const double2 l = Lt[((size_t)sg * ntk + slot[v]) * nec + e];
+            L[v] = cx(l.x, l.y);
+          }
+          normal_terms(nc, dsgn, z, L, x);
         }
-        normal_terms(nc, z2, z3, L, ffk, x);
+#pragma unroll
+        for (int v = 0; v < 4; v++) acc[v] = sg == 0 ? x[v] : acc[v] + x[v];
       }
-      for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], x[v]);
+#pragma unroll
+      for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], acc[v]);
     }
   }
   // near-degenerate or Fermi-cut tetrahedra: the reference's forms
-  for (int idx = threadIdx.x; idx < n_other; idx += blockDim.x) {
-    const int code = lists[2 * ntet - 1 - idx], t = code >> 1, sg = code & 1;
-    const double dsgn = sg == 0 ? 1.0 : -1.0;
-    int slot[4];
-    double ee1[4], ee2[4];
-    for (int v = 0; v < 4; v++) { slot[v] = a.imt1[4 * t + v]; ee1[v] = e1m[slot[v]]; ee2[v] = e2m[slot[v]]; }
-    const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
-    const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
-    if (mn2 > f && mx1 < f) {
-      cx ffk[4], ggk[4];
-      for (int v = 0; v < 4; v++) { ffk[v] = cx(dsgn, 0); ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn; }
-      if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, nullptr, xo)) atomicExch(a.err, 2);
-      continue;
-    }
-    double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
-    for (int i = 0; i < 4; i++)
-      for (int v = 0; v < 4; v++) dwgt[0][i][v] = (i == v) ? 1.0 : 0.0;
-    dvol[0] = 1.0;
-    int nt = 1;
-    if (!ttct(f, ee2, +1, nt, dwgt, dvol) || !ttct(f, ee1, -1, nt, dwgt, dvol)) { atomicExch(a.err, 1); continue; }
-    for (int i3 = 0; i3 < nt; i3++) {
-      cx ffk[4], ggk[4];
-      for (int i4 = 0; i4 < 4; i4++) {
-        double sm = 0;
-        for (int v = 0; v < 4; v++) sm += (ee2[v] - ee1[v]) * dwgt[i3][i4][v];
-        ffk[i4] = cx(dvol[i3], 0) * dsgn;
-        ggk[i4] = cx(-sm, delt) * dsgn;
-      }
-      double w4[4][4];
-      for (int i4 = 0; i4 < 4; i4++)
-        for (int v = 0; v < 4; v++) w4[i4][v] = dwgt[i3][i4][v];
-      if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, w4, xo)) atomicExch(a.err, 2);
-    }
-  }
+  for (int idx = threadIdx.x; idx < n_other; idx += blockDim.x)
+    other_tetra(a, lists[2 * ntet - 1 - idx], e1m, e2m, Lt, e0, ne, nec, xo);
   __syncthreads();
   // w[(p*nen + e)*ntk + k] = xow(mesh(k), e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
   for (int i = threadIdx.x; i < ntk * ne; i += blockDim.x) {
