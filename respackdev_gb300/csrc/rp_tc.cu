@@ -21,17 +21,20 @@
 // smaller, go to a second accumulator.  After each sub-chunk the epilogue
 // warps add both, times the rows' scales, into an FP64 copy of the tile.
 //
-// Kernel layout (one CTA per (frequency, upper tile)), 288 threads:
-//   warps 0-3  producers: read FP32 rho and the weights, scale, split and store
-//              the operand tiles into shared memory in the 128-byte-swizzled
-//              K-major layout the tensor core reads;
-//   warps 4-7  epilogue: drain the FP32 accumulators from tensor memory
-//              (tcgen05.ld) into the FP64 tile;
-//   warp 8     allocates tensor memory and issues tcgen05.mma (one thread).
-// Two operand stages and two accumulator buffers (2 channels x 128 columns
-// each, all 512 TMEM columns) overlap production, MMA and draining.  Every
-// mbarrier wait is bounded; on timeout the CTA raises the error word, waits
-// (bounded) for its own MMAs and frees tensor memory before returning.
+// Kernel layout: one CTA per (upper tile, frequency, Re/Im weight), 448 threads.
+//   warps 0-7   producers: read the FP32 rows of the A operand (prefetched one K
+//               block ahead in registers), multiply by the weights, split into
+//               planes and store them into shared memory in the 128-byte-swizzled
+//               K-major layout the tensor core reads;
+//   warps 8-11  epilogue: drain the FP32 accumulators from tensor memory
+//               (tcgen05.ld) into a float-pair running sum, then the FP64 tile;
+//   warp 12     allocates tensor memory and issues tcgen05.mma (one thread);
+//   warp 13     loader (one thread): bulk-copies (cp.async.bulk) the B operand
+//               planes -- split once per batch by bplanes_kernel and shared by
+//               every channel -- and the block's weights into the stage.
+// Two operand stages overlap loading, production and MMA.  Every mbarrier wait
+// is bounded; on timeout the CTA raises the error word, waits (bounded) for its
+// own MMAs and bulk copies and frees tensor memory before returning.
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -51,9 +54,10 @@ constexpr int BN = 128;          // tile columns (b)
 constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
 constexpr int NSTAGE = 2;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
-constexpr int NPROD = 256, NEPI = 128;    // 8 producer warps, 4 epilogue warps, 1 MMA warp
+constexpr int NPROD = 256, NEPI = 128;    // 8 producer warps, 4 epilogue warps, MMA warp, loader warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
-constexpr int NTHREADS = NPROD + NEPI + 32;
+constexpr int NTHREADS = NPROD + NEPI + 64;
+constexpr int WBYTES = BK * 16;            // weights of one K block (float4 per K)
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
 struct TcArgs {
@@ -66,8 +70,8 @@ struct TcArgs {
   double *M64;            // [nen][2][Mp][Mp] FP64 tiles (upper triangle used)
   int *err;
   int Mp, Kp, nen, ntile_side, ksub_blocks, nplanes, bf16;
-  int nch;                // channels (Re / Im weight) per CTA: 2, or 1 (grid.y = 2 nen)
   const int2 *tiles;      // (ta, tb) list, ta <= tb
+  const unsigned char *Bp;  // B operand planes, [tb][kb][plane] tiles of TILE_BYTES
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -195,34 +199,84 @@ __device__ __forceinline__ void split_t(float v, float vl, uint16_t (&t)[NP]) {
   }
 }
 
-// NP operand planes, NCH channels per CTA, EXACT integer leading plane, BF16 or FP16
-template <int NP, int NCH, bool EXACT, bool BF16>
+// B operand planes of the batch, once for every channel: Bp[((tb*nkb + kb)*NP + p)*TILE_BYTES]
+// holds rows tb*128.. of plane p for K block kb in the swizzled layout the
+// tensor core reads (the same split as the A operand, without a weight).
+template <int NP, bool EXACT, bool BF16>
+__global__ void __launch_bounds__(256) bplanes_kernel(const float *__restrict__ Yt, const float *__restrict__ sB, int Kp,
+                                                      int nkb, unsigned char *__restrict__ Bp) {
+  const int tb = blockIdx.y, kb = blockIdx.x, tid = threadIdx.x;
+  const int r = tid & (BM - 1), half = tid >> 7;
+  const float s = sB[tb * BM + r];
+  const float *y = Yt + (size_t)(tb * BM + r) * Kp + (size_t)kb * BK;
+  unsigned char *dst = Bp + ((size_t)tb * nkb + kb) * NP * TILE_BYTES;
+#pragma unroll 1
+  for (int cc = 0; cc < 4; cc++) {
+    const int c = 4 * half + cc;
+    const float4 v0 = __ldg((const float4 *)(y + 8 * c)), v1 = __ldg((const float4 *)(y + 8 * c) + 1);
+    const float bv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+    uint32_t wb[NP][4];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      uint16_t t[NP];
+      split_t<NP, EXACT, BF16>(bv[j] * s, 0.f, t);
+#pragma unroll
+      for (int p = 0; p < NP; p++) {
+        if (j & 1) wb[p][j >> 1] |= (uint32_t)t[p] << 16;
+        else wb[p][j >> 1] = t[p];
+      }
+    }
+    const uint32_t off = swz(r, c);
+#pragma unroll
+    for (int p = 0; p < NP; p++)
+      *(uint4 *)(dst + (size_t)p * TILE_BYTES + off) = make_uint4(wb[p][0], wb[p][1], wb[p][2], wb[p][3]);
+  }
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t *b, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+// bulk copy global -> shared, completion counted in bytes on mbarrier b
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(b))
+               : "memory");
+}
+
+// NP operand planes, EXACT integer leading plane, BF16 or FP16.  One CTA per
+// (upper tile, frequency, Re/Im weight); see the file comment for the roles.
+template <int NP, bool EXACT, bool BF16>
 __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-align the operand area
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  constexpr int TPS = NP * (1 + NCH);        // tiles per stage: B planes + NCH x A planes
-  constexpr int NACC = EXACT ? 2 : 1;        // accumulators per channel
+  constexpr int NACC = EXACT ? 2 : 1;               // accumulators
+  constexpr int AOFF = 0, BOFF = NP * TILE_BYTES, WOFF = 2 * NP * TILE_BYTES;
+  constexpr int STAGE = 2 * NP * TILE_BYTES + WBYTES;
   unsigned char *stage_base = smem;
-  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * TPS * TILE_BYTES);
-  uint64_t *full = bars, *empty = bars + 2, *accfull = bars + 4, *accempty = bars + 6, *fin = bars + 8;
-  volatile int *abort_flag = (volatile int *)(bars + 9);
-  uint32_t *tmem_slot = (uint32_t *)(bars + 10);
+  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * STAGE);
+  uint64_t *full = bars, *wfull = bars + 2, *empty = bars + 4, *accfull = bars + 6, *accempty = bars + 8,
+           *fin = bars + 10;
+  volatile int *abort_flag = (volatile int *)(bars + 11);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 12);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // frequency e and the first channel handled here (channel 0 = Re weight, 1 = Im weight)
-  const int e = NCH == 2 ? blockIdx.y : blockIdx.y >> 1;
-  const int ch0 = NCH == 2 ? 0 : (blockIdx.y & 1);
+  const int e = blockIdx.y >> 1, ch = blockIdx.y & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
   const int2 tt = a.tiles[blockIdx.x];
   const int ta = tt.x, tb = tt.y;
   const int nkb = a.Kp / BK;
   const int nsub = (nkb + a.ksub_blocks - 1) / a.ksub_blocks;
 
   if (tid == 0) {
-    mbar_init(&full[0], NPROD); mbar_init(&full[1], NPROD);
-    mbar_init(&empty[0], 1); mbar_init(&empty[1], 1);
-    mbar_init(&accfull[0], 1); mbar_init(&accfull[1], 1);
-    mbar_init(&accempty[0], NEPI); mbar_init(&accempty[1], NEPI);
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&full[s], NPROD);
+      mbar_init(&wfull[s], 1);
+      mbar_init(&empty[s], 1);
+      mbar_init(&accfull[s], 1);
+      mbar_init(&accempty[s], NEPI);
+    }
     mbar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -236,102 +290,88 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int cbase = 2 * e + ch0;  // channel index of lc = 0
+  const int cidx = 2 * e + ch;
 
   if (warp < NPROD / 32) {
-    // ---------------- producers: two threads per operand row, 32 K each ----------------
+    // ---------------- producers: the weighted A operand, two threads per row ----------------
     const int r = tid & (BM - 1), half = tid >> 7;
-    const float sB = a.sB[tb * BM + r];
-    float sA[NCH];
+    const float sA = a.sA[(size_t)cidx * a.Mp + ta * BM + r];
+    const float4 *ya = (const float4 *)(a.Yt + (size_t)(ta * BM + r) * a.Kp) + 8 * half;
+    float4 cur[8], nxt[8];
 #pragma unroll
-    for (int lc = 0; lc < NCH; lc++) sA[lc] = a.sA[(size_t)(cbase + lc) * a.Mp + ta * BM + r];
-    const float *ya = a.Yt + (size_t)(ta * BM + r) * a.Kp;
-    const float *yb = a.Yt + (size_t)(tb * BM + r) * a.Kp;
-    const float4 *wt = a.wt + (size_t)e * a.Kp;
+    for (int i = 0; i < 8; i++) cur[i] = __ldg(ya + i);
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
+      if (kb + 1 < nkb) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) nxt[i] = __ldg(ya + (size_t)(kb + 1) * (BK / 4) + i);
+      }
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
-      unsigned char *st = stage_base + (size_t)s * TPS * TILE_BYTES;
-      const int k0 = kb * BK;
-#pragma unroll 1
-      for (int cc = 0; cc < 4; cc++) {  // this thread's 4 chunks of 8 K values
+      if (!mbar_wait(&wfull[s], use & 1, abort_flag)) break;  // weights of this block
+      unsigned char *st = stage_base + (size_t)s * STAGE;
+      const float4 *wsm = (const float4 *)(st + WOFF);
+      // fully unrolled: cur[] must be indexed by constants to stay in registers
+#pragma unroll
+      for (int cc = 0; cc < 4; cc++) {
         const int c = 4 * half + cc;
-        const float4 *pa = (const float4 *)(ya + k0 + 8 * c), *pb = (const float4 *)(yb + k0 + 8 * c);
-        const float4 a0 = __ldg(pa), a1 = __ldg(pa + 1), b0 = __ldg(pb), b1 = __ldg(pb + 1);
-        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
-        uint32_t wb[NP][4], wa[NCH][NP][4];
+        const float av[8] = {cur[2 * cc].x, cur[2 * cc].y, cur[2 * cc].z, cur[2 * cc].w,
+                             cur[2 * cc + 1].x, cur[2 * cc + 1].y, cur[2 * cc + 1].z, cur[2 * cc + 1].w};
+        uint32_t wa[NP][4];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          const float4 w = __ldg(wt + k0 + 8 * c + j);
+          const float4 w = wsm[8 * c + j];
+          // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
+          const float xs = (ch == 0 ? w.x : w.z) * sA, xl = (ch == 0 ? w.y : w.w) * sA;
+          const float zh = xs * av[j];
+          const float zl = fmaf(xl, av[j], fmaf(xs, av[j], -zh));
           uint16_t t[NP];
-          split_t<NP, EXACT, BF16>(bv[j] * sB, 0.f, t);
+          split_t<NP, EXACT, BF16>(zh, zl, t);
 #pragma unroll
           for (int p = 0; p < NP; p++) {
-            if (j & 1) wb[p][j >> 1] |= (uint32_t)t[p] << 16;
-            else wb[p][j >> 1] = t[p];
-          }
-#pragma unroll
-          for (int lc = 0; lc < NCH; lc++) {
-            const int ch = ch0 + lc;
-            // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
-            const float xs = (ch == 0 ? w.x : w.z) * sA[lc], xl = (ch == 0 ? w.y : w.w) * sA[lc];
-            const float zh = xs * av[j];
-            const float zl = fmaf(xl, av[j], fmaf(xs, av[j], -zh));
-            split_t<NP, EXACT, BF16>(zh, zl, t);
-#pragma unroll
-            for (int p = 0; p < NP; p++) {
-              if (j & 1) wa[lc][p][j >> 1] |= (uint32_t)t[p] << 16;
-              else wa[lc][p][j >> 1] = t[p];
-            }
+            if (j & 1) wa[p][j >> 1] |= (uint32_t)t[p] << 16;
+            else wa[p][j >> 1] = t[p];
           }
         }
         const uint32_t off = swz(r, c);
 #pragma unroll
-        for (int p = 0; p < NP; p++) {
-          *(uint4 *)(st + (size_t)p * TILE_BYTES + off) = make_uint4(wb[p][0], wb[p][1], wb[p][2], wb[p][3]);
-#pragma unroll
-          for (int lc = 0; lc < NCH; lc++)
-            *(uint4 *)(st + (size_t)(NP * (1 + lc) + p) * TILE_BYTES + off) =
-                make_uint4(wa[lc][p][0], wa[lc][p][1], wa[lc][p][2], wa[lc][p][3]);
-        }
+        for (int p = 0; p < NP; p++)
+          *(uint4 *)(st + AOFF + (size_t)p * TILE_BYTES + off) = make_uint4(wa[p][0], wa[p][1], wa[p][2], wa[p][3]);
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
+#pragma unroll
+      for (int i = 0; i < 8; i++) cur[i] = nxt[i];
     }
   } else if (warp < MMA_WARP) {
     // ---------------- epilogue: fold each sub-chunk into a float-pair accumulator ----------------
-    // TMEM columns per channel: [main][corr (exact scheme)][acc hi][acc lo], 128 each.
+    // TMEM columns: [main][corr (exact scheme)][acc hi][acc lo], 128 each.
     // acc = hi + lo is updated with an error-free TwoSum, so the running sum keeps
     // about 48 bits with FP32 arithmetic only; the FP64 tile is written once.
     const int q = warp & 3;                 // this warp may read TMEM lanes 32q..32q+31
     const int row = ta * BM + 32 * q + lane;
     const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
+    const uint32_t cm = 0, cc = BN, chi = NACC * BN, clo = chi + BN;
     for (int sc = 0; sc < nsub; sc++) {
       if (!mbar_wait(&accfull[0], sc & 1, abort_flag)) break;
       tc_fence_after();
 #pragma unroll 1
-      for (int lc = 0; lc < NCH; lc++) {
-        const uint32_t cm = (uint32_t)(lc * (NACC + 2)) * BN, cc = cm + BN, ch = cm + NACC * BN, cl = ch + BN;
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-          float m[16], cr[16], hi[16], lo[16];
-          tmem_ld16(lanebase + cm + c0, m);
-          if (NACC == 2) tmem_ld16(lanebase + cc + c0, cr);
-          if (sc > 0) { tmem_ld16(lanebase + ch + c0, hi); tmem_ld16(lanebase + cl + c0, lo); }
-          tmem_wait_ld();
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float m[16], cr[16], hi[16], lo[16];
+        tmem_ld16(lanebase + cm + c0, m);
+        if (NACC == 2) tmem_ld16(lanebase + cc + c0, cr);
+        if (sc > 0) { tmem_ld16(lanebase + chi + c0, hi); tmem_ld16(lanebase + clo + c0, lo); }
+        tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 16; j++) {
-            const float a0 = sc > 0 ? hi[j] : 0.f, l0 = sc > 0 ? lo[j] : 0.f;
-            const float x = m[j];
-            const float sm = a0 + x, bb = sm - a0;
-            const float err = (a0 - (sm - bb)) + (x - bb);
-            hi[j] = sm;
-            lo[j] = l0 + err + (NACC == 2 ? cr[j] : 0.f);
-          }
-          tmem_st16(lanebase + ch + c0, hi);
-          tmem_st16(lanebase + cl + c0, lo);
+        for (int j = 0; j < 16; j++) {
+          const float a0 = sc > 0 ? hi[j] : 0.f, l0 = sc > 0 ? lo[j] : 0.f;
+          const float x = m[j];
+          const float sm = a0 + x, bb = sm - a0;
+          const float err = (a0 - (sm - bb)) + (x - bb);
+          hi[j] = sm;
+          lo[j] = l0 + err + (NACC == 2 ? cr[j] : 0.f);
         }
+        tmem_st16(lanebase + chi + c0, hi);
+        tmem_st16(lanebase + clo + c0, lo);
       }
       tmem_wait_st();
       tc_fence_before();
@@ -340,42 +380,39 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
     // the batch's sum, unscaled, into the FP64 tile
     if (!*abort_flag) {
       tc_fence_after();
+      const double ia = 1.0 / (double)a.sA[(size_t)cidx * a.Mp + row];
+      double *dst = a.M64 + (((size_t)e * 2 + ch) * a.Mp + row) * a.Mp + tb * BN;
+      const float *sbc = a.sB + tb * BN;
 #pragma unroll 1
-      for (int lc = 0; lc < NCH; lc++) {
-        const uint32_t ch = (uint32_t)(lc * (NACC + 2) + NACC) * BN, cl = ch + BN;
-        const double ia = 1.0 / (double)a.sA[(size_t)(cbase + lc) * a.Mp + row];
-        double *dst = a.M64 + (((size_t)e * 2 + ch0 + lc) * a.Mp + row) * a.Mp + tb * BN;
-        const float *sbc = a.sB + tb * BN;
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-          float hi[16], lo[16];
-          tmem_ld16(lanebase + ch + c0, hi);
-          tmem_ld16(lanebase + cl + c0, lo);
-          tmem_wait_ld();
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        float hi[16], lo[16];
+        tmem_ld16(lanebase + chi + c0, hi);
+        tmem_ld16(lanebase + clo + c0, lo);
+        tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 16; j++) dst[c0 + j] += ((double)hi[j] + (double)lo[j]) * ia / (double)sbc[c0 + j];
-        }
+        for (int j = 0; j < 16; j++) dst[c0 + j] += ((double)hi[j] + (double)lo[j]) * ia / (double)sbc[c0 + j];
       }
     }
-  } else if (lane == 0) {
-    // ---------------- MMA issuer ----------------
-    const uint32_t idesc = make_idesc(BF16 ? 1 : 0, BM, BN);
-    for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
-      // the epilogue must have read the previous sub-chunk's sums
-      if (sc > 0 && !mbar_wait(&accempty[0], (sc - 1) & 1, abort_flag)) break;
-      tc_fence_after();
-      const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
-      bool ok = true;
-      for (int kb = kbeg; kb < kend; kb++) {
-        const int s = kb & 1, use = kb >> 1;
-        if (!mbar_wait(&full[s], use & 1, abort_flag)) { ok = false; break; }
+  } else if (warp == MMA_WARP) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      const uint32_t idesc = make_idesc(BF16 ? 1 : 0, BM, BN);
+      for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
+        // the epilogue must have read the previous sub-chunk's sums
+        if (sc > 0 && !mbar_wait(&accempty[0], (sc - 1) & 1, abort_flag)) break;
         tc_fence_after();
-        const uint32_t st = smem_u32(stage_base + (size_t)s * TPS * TILE_BYTES);
+        const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
+        bool ok = true;
+        for (int kb = kbeg; kb < kend; kb++) {
+          const int s = kb & 1, use = kb >> 1;
+          if (!mbar_wait(&wfull[s], use & 1, abort_flag) || !mbar_wait(&full[s], use & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t st = smem_u32(stage_base + (size_t)s * STAGE);
 #pragma unroll
-        for (int kk = 0; kk < BK / 16; kk++)
-#pragma unroll
-          for (int lc = 0; lc < NCH; lc++) {
-            const uint32_t d0 = tmem + (uint32_t)(lc * (NACC + 2)) * BN;
+          for (int kk = 0; kk < BK / 16; kk++) {
             const bool fresh = (kb == kbeg && kk == 0);
             int idx0 = 0, idx1 = 0;
             // products of planes pa (A) and pb (B) with pa + pb <= NP - 1; with the
@@ -384,25 +421,48 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
             for (int pa = 0; pa < NP; pa++)
 #pragma unroll
               for (int pb = 0; pa + pb < NP; pb++) {
-                const uint64_t ad = make_desc(st + (uint32_t)((NP * (1 + lc) + pa) * TILE_BYTES) + kk * 32);
-                const uint64_t bd = make_desc(st + (uint32_t)(pb * TILE_BYTES) + kk * 32);
+                const uint64_t ad = make_desc(st + (uint32_t)(AOFF + pa * TILE_BYTES) + kk * 32);
+                const uint64_t bd = make_desc(st + (uint32_t)(BOFF + pb * TILE_BYTES) + kk * 32);
                 if ((EXACT && pa == 0 && pb == 0) || !EXACT) {
-                  mma_f16(d0, ad, bd, idesc, (fresh && idx0 == 0) ? 0 : 1);
+                  mma_f16(tmem, ad, bd, idesc, (fresh && idx0 == 0) ? 0 : 1);
                   idx0++;
                 } else {
-                  mma_f16(d0 + BN, ad, bd, idesc, (fresh && idx1 == 0) ? 0 : 1);
+                  mma_f16(tmem + BN, ad, bd, idesc, (fresh && idx1 == 0) ? 0 : 1);
                   idx1++;
                 }
               }
           }
-        mma_commit(&empty[s]);
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&accfull[0]);
       }
-      if (!ok) break;
-      mma_commit(&accfull[0]);
+      // wait for every MMA this thread issued before tensor memory is released
+      mma_commit(fin);
+      mbar_wait(fin, 0, abort_flag);
     }
-    // wait for every MMA this thread issued before tensor memory is released
-    mma_commit(fin);
-    mbar_wait(fin, 0, abort_flag);
+  } else if (lane == 0) {
+    // ---------------- loader: B planes and the block's weights by bulk copy ----------------
+    const unsigned char *bsrc = a.Bp + (size_t)tb * nkb * NP * TILE_BYTES;
+    const float4 *wsrc = a.wt + (size_t)e * a.Kp;
+    int issued = 0;
+    for (int kb = 0; kb < nkb; kb++) {
+      const int s = kb & 1, use = kb >> 1;
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
+      unsigned char *st = stage_base + (size_t)s * STAGE;
+      mbar_arrive_tx(&wfull[s], (uint32_t)(NP * TILE_BYTES + WBYTES));
+#pragma unroll
+      for (int p = 0; p < NP; p++)
+        bulk_g2s(st + BOFF + p * TILE_BYTES, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, TILE_BYTES, &wfull[s]);
+      bulk_g2s(st + WOFF, wsrc + (size_t)kb * BK, WBYTES, &wfull[s]);
+      issued = kb + 1;
+    }
+    // after an abort, wait (bounded) for the copies still in flight before the CTA exits
+    if (*abort_flag) {
+      for (int kb = max(0, issued - NSTAGE); kb < issued; kb++) {
+        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&wfull[kb & 1], (kb >> 1) & 1); i++) __nanosleep(32);
+      }
+    }
   }
   __syncwarp();
   if (tid == 0 && *abort_flag) atomicExch(a.err, 4);
@@ -601,16 +661,20 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   const int Gp = Gp_of(ng), Mp = 2 * Gp;
   const long Kn = (long)npair * ntk;
   const int Kp = (int)(((Kn + BK - 1) / BK) * BK);
-  // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float2, maxes
+  const int nplanes = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2;
+  // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float4, maxes, scales, B planes
   const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float4) * (size_t)nen * Kp;
   const size_t mxbytes = sizeof(float) * (1 + 2 * (size_t)nen);
   const size_t sbytes = sizeof(float) * (size_t)Mp * (2 + 2 * (size_t)nen);  // rowmax, sB, sA
-  unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, ybytes + wbytes + mxbytes + sbytes + 512);
+  const size_t bpbytes = (size_t)nplanes * 2 * Mp * Kp;
+  const size_t sboff = ((ybytes + wbytes + ((mxbytes + 255) / 256) * 256 + sbytes + 1023) / 1024) * 1024;
+  unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, sboff + bpbytes + 1024);
   float *Yt = (float *)base;
   float4 *wt = (float4 *)(base + ybytes);
   float *maxes = (float *)(base + ybytes + wbytes);
   float *rowmax = (float *)(base + ybytes + wbytes + ((mxbytes + 255) / 256) * 256);
   float *sBv = rowmax + Mp, *sAv = sBv + Mp;
+  unsigned char *Bp = base + sboff;
   RP_CUDA(cudaMemsetAsync(base, 0, ybytes + wbytes + mxbytes, st));
   if (Kn > 0x7fffffffL) fail(1, "batch too large");
   if (rho64) yt_kernel<double2><<<(unsigned)Kn, 128, 0, st>>>(rho64, npair, ntk, ng, Gp, Kp, Yt, head, g0);
@@ -638,29 +702,37 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   grow(d_tiles, d_tiles_bytes, sizeof(int2) * tl.size());
   RP_CUDA(cudaMemcpyAsync(d_tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, st));
   note_transfer((long long)(sizeof(int2) * tl.size()), 0);
+  // B operand planes, shared by every (frequency, Re/Im) channel
+  const int nkb = Kp / BK;
+  {
+    dim3 g((unsigned)nkb, nt);
+    if (precision == RP_PREC_FP16X3) bplanes_kernel<3, true, false><<<g, 256, 0, st>>>(Yt, sBv, Kp, nkb, Bp);
+    else if (precision == RP_PREC_BF16X3) bplanes_kernel<3, true, true><<<g, 256, 0, st>>>(Yt, sBv, Kp, nkb, Bp);
+    else bplanes_kernel<2, false, false><<<g, 256, 0, st>>>(Yt, sBv, Kp, nkb, Bp);
+    launches++;
+    RP_CUDA(cudaGetLastError());
+  }
   TcArgs a;
   a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.M64 = (double *)ws.part; a.err = err;
   a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;
-  a.nplanes = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2;
+  a.nplanes = nplanes;
   a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
   a.exact = exact;
   a.sB = sBv; a.sA = sAv;
-  // one channel per CTA: main (+ correction) accumulators and the float-pair
-  // running sum take 3 or 4 x 128 of the 512 TMEM columns
-  a.nch = 1;
+  a.Bp = Bp;
   // default 1024 K per FP32 sub-chunk: integer partial sums must stay below 2^24
   a.ksub_blocks = ws.ksub > 0 ? ws.ksub : 16;
   if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
-  const int tiles_per_stage = a.nplanes * (1 + a.nch);
-  const size_t smem = 1024 + (size_t)NSTAGE * tiles_per_stage * TILE_BYTES + 128;
+  // per stage: A planes, B planes, the block's weights; then the barriers
+  const size_t smem = 1024 + (size_t)NSTAGE * (2 * (size_t)nplanes * TILE_BYTES + WBYTES) + 128;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
   void (*kern)(TcArgs);
-  if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, 1, true, false>;
-  else if (precision == RP_PREC_BF16X3) kern = tc_gram_kernel<3, 1, true, true>;
-  else kern = tc_gram_kernel<2, 1, false, false>;
+  if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, true, false>;
+  else if (precision == RP_PREC_BF16X3) kern = tc_gram_kernel<3, true, true>;
+  else kern = tc_gram_kernel<2, false, false>;
   RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)tl.size(), nen * (2 / a.nch));
+  dim3 grid((unsigned)tl.size(), 2 * nen);
   RP_CUDA(cudaEventRecord(ws.ev0, st));
   kern<<<grid, NTHREADS, smem, st>>>(a);
   RP_CUDA(cudaEventRecord(ws.ev1, st));
