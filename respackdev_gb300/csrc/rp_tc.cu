@@ -261,6 +261,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
            *fin = bars + 10;
   volatile int *abort_flag = (volatile int *)(bars + 11);
   uint32_t *tmem_slot = (uint32_t *)(bars + 12);
+  float *sA_s = (float *)(bars + 16);               // row scales of this CTA's A rows (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int e = blockIdx.y >> 1, ch = blockIdx.y & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
@@ -291,56 +292,55 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int cidx = 2 * e + ch;
+  for (int i = tid; i < BM; i += NTHREADS) sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
+  __syncthreads();
 
   if (warp < NPROD / 32) {
-    // ---------------- producers: the weighted A operand, two threads per row ----------------
-    const int r = tid & (BM - 1), half = tid >> 7;
-    const float sA = a.sA[(size_t)cidx * a.Mp + ta * BM + r];
-    const float4 *ya = (const float4 *)(a.Yt + (size_t)(ta * BM + r) * a.Kp) + 8 * half;
-    float4 cur[8], nxt[8];
+    // ---------------- producers: the weighted A operand ----------------
+    // warp pw owns rows 16 pw .. 16 pw + 15; lane l the K pair 2l, 2l+1 of every
+    // block, so the global reads are coalesced (one 256-byte row per instruction),
+    // the lane's two weights serve all 16 rows, and each plane store writes one
+    // full 128-byte swizzled row.
+    const int pw = warp, r0 = 16 * pw;
+    const float2 *ya = (const float2 *)(a.Yt + (size_t)(ta * BM + r0) * a.Kp) + lane;
+    const size_t rstride = (size_t)a.Kp / 2;  // float2 per row
+    float2 cur[16], nxt[16];
 #pragma unroll
-    for (int i = 0; i < 8; i++) cur[i] = __ldg(ya + i);
+    for (int i = 0; i < 16; i++) cur[i] = __ldg(ya + i * rstride);
+    const uint32_t cofs = (uint32_t)(lane & 3) * 4, chunk = (uint32_t)(lane >> 2);
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
       if (kb + 1 < nkb) {
 #pragma unroll
-        for (int i = 0; i < 8; i++) nxt[i] = __ldg(ya + (size_t)(kb + 1) * (BK / 4) + i);
+        for (int i = 0; i < 16; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
       }
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
       if (!mbar_wait(&wfull[s], use & 1, abort_flag)) break;  // weights of this block
       unsigned char *st = stage_base + (size_t)s * STAGE;
       const float4 *wsm = (const float4 *)(st + WOFF);
-      // fully unrolled: cur[] must be indexed by constants to stay in registers
+      const float4 w0 = wsm[2 * lane], w1 = wsm[2 * lane + 1];
+      const float x0h = ch == 0 ? w0.x : w0.z, x0l = ch == 0 ? w0.y : w0.w;
+      const float x1h = ch == 0 ? w1.x : w1.z, x1l = ch == 0 ? w1.y : w1.w;
 #pragma unroll
-      for (int cc = 0; cc < 4; cc++) {
-        const int c = 4 * half + cc;
-        const float av[8] = {cur[2 * cc].x, cur[2 * cc].y, cur[2 * cc].z, cur[2 * cc].w,
-                             cur[2 * cc + 1].x, cur[2 * cc + 1].y, cur[2 * cc + 1].z, cur[2 * cc + 1].w};
-        uint32_t wa[NP][4];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const float4 w = wsm[8 * c + j];
-          // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
-          const float xs = (ch == 0 ? w.x : w.z) * sA, xl = (ch == 0 ? w.y : w.w) * sA;
-          const float zh = xs * av[j];
-          const float zl = fmaf(xl, av[j], fmaf(xs, av[j], -zh));
-          uint16_t t[NP];
-          split_t<NP, EXACT, BF16>(zh, zl, t);
-#pragma unroll
-          for (int p = 0; p < NP; p++) {
-            if (j & 1) wa[p][j >> 1] |= (uint32_t)t[p] << 16;
-            else wa[p][j >> 1] = t[p];
-          }
-        }
-        const uint32_t off = swz(r, c);
+      for (int i = 0; i < 16; i++) {
+        const int row = r0 + i;
+        // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
+        const float sa = sA_s[r0 + i];
+        const float xs0 = x0h * sa, xl0 = x0l * sa, xs1 = x1h * sa, xl1 = x1l * sa;
+        const float zh0 = xs0 * cur[i].x, zl0 = fmaf(xl0, cur[i].x, fmaf(xs0, cur[i].x, -zh0));
+        const float zh1 = xs1 * cur[i].y, zl1 = fmaf(xl1, cur[i].y, fmaf(xs1, cur[i].y, -zh1));
+        uint16_t t0[NP], t1[NP];
+        split_t<NP, EXACT, BF16>(zh0, zl0, t0);
+        split_t<NP, EXACT, BF16>(zh1, zl1, t1);
+        const uint32_t off = (uint32_t)row * 128 + ((chunk ^ (uint32_t)(row & 7)) << 4) + cofs;
 #pragma unroll
         for (int p = 0; p < NP; p++)
-          *(uint4 *)(st + AOFF + (size_t)p * TILE_BYTES + off) = make_uint4(wa[p][0], wa[p][1], wa[p][2], wa[p][3]);
+          *(uint32_t *)(st + AOFF + (size_t)p * TILE_BYTES + off) = (uint32_t)t0[p] | ((uint32_t)t1[p] << 16);
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
 #pragma unroll
-      for (int i = 0; i < 8; i++) cur[i] = nxt[i];
+      for (int i = 0; i < 16; i++) cur[i] = nxt[i];
     }
   } else if (warp < MMA_WARP) {
     // ---------------- epilogue: fold each sub-chunk into a float-pair accumulator ----------------
@@ -725,7 +725,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
   // per stage: A planes, B planes, the block's weights; then the barriers
-  const size_t smem = 1024 + (size_t)NSTAGE * (2 * (size_t)nplanes * TILE_BYTES + WBYTES) + 128;
+  const size_t smem = 1024 + (size_t)NSTAGE * (2 * (size_t)nplanes * TILE_BYTES + WBYTES) + 128 + sizeof(float) * BM;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
   void (*kern)(TcArgs);
   if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, true, false>;
