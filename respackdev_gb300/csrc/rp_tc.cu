@@ -185,17 +185,48 @@ __device__ __forceinline__ uint32_t swz(int row, int chunk16) {
   return (uint32_t)(row * 128 + ((chunk16 ^ (row & 7)) << 4));
 }
 
+// Split two values (each a float pair v + l, l joining after the leading term)
+// into NP planes, packed two per 32-bit word.  Built from full-rate FP32
+// operations; the only conversions are the packed cvt.rn.{f16,bf16}x2 stores:
+//   integer leading plane: round to nearest even by adding and removing 1.5 * 2^23
+//     (exact for |v| < 2^22);
+//   16-bit planes: Veltkamp splitting (t = v (2^s + 1); h = t - (t - v)) rounds v
+//     to the 11 (FP16) or 8 (BF16) significant bits the plane holds, so v - h is
+//     exact; __fmul_rn / __fsub_rn keep the compiler from fusing the steps;
+//   last plane: the remainder itself, rounded by the conversion.
+template <bool BF16>
+__device__ __forceinline__ float round_to_plane(float v) {
+  const float t = __fmul_rn(v, BF16 ? 65537.0f : 8193.0f);
+  return __fsub_rn(t, __fsub_rn(t, v));
+}
+template <bool BF16>
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  if (BF16) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *(const uint32_t *)&h;
+  }
+  const __half2 h = __floats2half2_rn(a, b);
+  return *(const uint32_t *)&h;
+}
 template <int NP, bool EXACT, bool BF16>
-__device__ __forceinline__ void split_t(float v, float vl, uint16_t (&t)[NP]) {
-  float r = v;
+__device__ __forceinline__ void split2(float v0, float l0, float v1, float l1, uint32_t (&w)[NP]) {
+  float r0 = v0, r1 = v1;
 #pragma unroll
   for (int p = 0; p < NP; p++) {
-    if (p == 1) r = r + vl;  // the low word joins once the leading term is removed
-    float h;
-    if (p == 0 && EXACT) h = rintf(r);
-    else h = BF16 ? __bfloat162float(__float2bfloat16_rn(r)) : __half2float(__float2half_rn(r));
-    t[p] = BF16 ? __bfloat16_as_ushort(__float2bfloat16_rn(h)) : __half_as_ushort(__float2half_rn(h));
-    r = r - h;
+    if (p == 1) { r0 = r0 + l0; r1 = r1 + l1; }
+    float h0, h1;
+    if (p == NP - 1) {
+      h0 = r0; h1 = r1;
+    } else if (p == 0 && EXACT) {
+      const float M = 12582912.0f;  // 1.5 * 2^23
+      h0 = __fsub_rn(__fadd_rn(r0, M), M);
+      h1 = __fsub_rn(__fadd_rn(r1, M), M);
+    } else {
+      h0 = round_to_plane<BF16>(r0);
+      h1 = round_to_plane<BF16>(r1);
+    }
+    w[p] = pack2<BF16>(h0, h1);
+    if (p < NP - 1) { r0 = __fsub_rn(r0, h0); r1 = __fsub_rn(r1, h1); }
   }
 }
 
@@ -217,14 +248,11 @@ __global__ void __launch_bounds__(256) bplanes_kernel(const float *__restrict__ 
     const float bv[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
     uint32_t wb[NP][4];
 #pragma unroll
-    for (int j = 0; j < 8; j++) {
-      uint16_t t[NP];
-      split_t<NP, EXACT, BF16>(bv[j] * s, 0.f, t);
+    for (int j = 0; j < 4; j++) {
+      uint32_t t[NP];
+      split2<NP, EXACT, BF16>(bv[2 * j] * s, 0.f, bv[2 * j + 1] * s, 0.f, t);
 #pragma unroll
-      for (int p = 0; p < NP; p++) {
-        if (j & 1) wb[p][j >> 1] |= (uint32_t)t[p] << 16;
-        else wb[p][j >> 1] = t[p];
-      }
+      for (int p = 0; p < NP; p++) wb[p][j] = t[p];
     }
     const uint32_t off = swz(r, c);
 #pragma unroll
@@ -238,6 +266,13 @@ __device__ __forceinline__ void mbar_arrive_tx(uint64_t *b, uint32_t bytes) {
                "r"(bytes)
                : "memory");
 }
+// L2 prefetch hints: a line for the producers' plain loads, a range for the loader's bulk copies
+__device__ __forceinline__ void prefetch_l2(const void *p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void bulk_prefetch_l2(const void *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+constexpr int PF_AHEAD = 4;  // K blocks between an L2 prefetch and its use
+
 // bulk copy global -> shared, completion counted in bytes on mbarrier b
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
@@ -314,6 +349,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
 #pragma unroll
         for (int i = 0; i < 16; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
       }
+      // DRAM -> L2 a few blocks ahead, one line per lane group: lanes 0 and 16 cover a row's 256 bytes
+      if (kb + PF_AHEAD < nkb && (lane & 15) == 0) {
+#pragma unroll
+        for (int i = 0; i < 16; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
+      }
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
       if (!mbar_wait(&wfull[s], use & 1, abort_flag)) break;  // weights of this block
       unsigned char *st = stage_base + (size_t)s * STAGE;
@@ -329,13 +369,11 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
         const float xs0 = x0h * sa, xl0 = x0l * sa, xs1 = x1h * sa, xl1 = x1l * sa;
         const float zh0 = xs0 * cur[i].x, zl0 = fmaf(xl0, cur[i].x, fmaf(xs0, cur[i].x, -zh0));
         const float zh1 = xs1 * cur[i].y, zl1 = fmaf(xl1, cur[i].y, fmaf(xs1, cur[i].y, -zh1));
-        uint16_t t0[NP], t1[NP];
-        split_t<NP, EXACT, BF16>(zh0, zl0, t0);
-        split_t<NP, EXACT, BF16>(zh1, zl1, t1);
+        uint32_t t[NP];
+        split2<NP, EXACT, BF16>(zh0, zl0, zh1, zl1, t);
         const uint32_t off = (uint32_t)row * 128 + ((chunk ^ (uint32_t)(row & 7)) << 4) + cofs;
 #pragma unroll
-        for (int p = 0; p < NP; p++)
-          *(uint32_t *)(st + AOFF + (size_t)p * TILE_BYTES + off) = (uint32_t)t0[p] | ((uint32_t)t1[p] << 16);
+        for (int p = 0; p < NP; p++) *(uint32_t *)(st + AOFF + (size_t)p * TILE_BYTES + off) = t[p];
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
@@ -450,6 +488,10 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       const int s = kb & 1, use = kb >> 1;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
+      if (kb + PF_AHEAD < nkb) {
+        bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
+        bulk_prefetch_l2(wsrc + (size_t)(kb + PF_AHEAD) * BK, WBYTES);
+      }
       mbar_arrive_tx(&wfull[s], (uint32_t)(NP * TILE_BYTES + WBYTES));
 #pragma unroll
       for (int p = 0; p < NP; p++)
