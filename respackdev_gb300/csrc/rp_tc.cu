@@ -57,7 +57,8 @@ constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
 constexpr int NPROD = 256, NEPI = 128;    // 8 producer warps, 4 epilogue warps, MMA warp, loader warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
-constexpr int WBYTES = BK * 16;            // weights of one K block (float4 per K)
+constexpr int WCHUNK = 16;                 // K blocks per weight chunk
+constexpr int WBYTES = WCHUNK * BK * 8;    // one channel's weights of a chunk (float2 per K)
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
 struct TcArgs {
@@ -65,7 +66,7 @@ struct TcArgs {
   const float *sB;        // [Mp] row scales of the unweighted operand
   const float *sA;        // [2 nen][Mp] row scales of the weighted operand per channel
   int exact;              // 1: integer leading plane + separate accumulator
-  const float4 *wt;       // [nen][Kp] weights as float pairs (re_hi, re_lo, im_hi, im_lo)
+  const float2 *wt;       // [nen][Re/Im][Kp] weights as float pairs (hi, lo)
   const float *maxes;     // [0] = max|Y|, [1 + 2e] = max|Re w_e|, [2 + 2e] = max|Im w_e|
   double *M64;            // [nen][2][Mp][Mp] FP64 tiles (upper triangle used)
   int *err;
@@ -288,15 +289,16 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
-  constexpr int AOFF = 0, BOFF = NP * TILE_BYTES, WOFF = 2 * NP * TILE_BYTES;
-  constexpr int STAGE = 2 * NP * TILE_BYTES + WBYTES;
+  constexpr int AOFF = 0, BOFF = NP * TILE_BYTES;
+  constexpr int STAGE = 2 * NP * TILE_BYTES;        // A planes, B planes
   unsigned char *stage_base = smem;
-  uint64_t *bars = (uint64_t *)(smem + (size_t)NSTAGE * STAGE);
-  uint64_t *full = bars, *wfull = bars + 2, *empty = bars + 4, *accfull = bars + 6, *accempty = bars + 8,
-           *fin = bars + 10;
-  volatile int *abort_flag = (volatile int *)(bars + 11);
-  uint32_t *tmem_slot = (uint32_t *)(bars + 12);
-  float *sA_s = (float *)(bars + 16);               // row scales of this CTA's A rows (128)
+  unsigned char *wring = smem + (size_t)NSTAGE * STAGE;  // two weight chunks
+  uint64_t *bars = (uint64_t *)(wring + 2 * WBYTES);
+  uint64_t *full = bars, *bfull = bars + 2, *empty = bars + 4, *accfull = bars + 6, *accempty = bars + 8,
+           *wready = bars + 10, *wfree = bars + 12, *fin = bars + 14;
+  volatile int *abort_flag = (volatile int *)(bars + 15);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 16);
+  float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int e = blockIdx.y >> 1, ch = blockIdx.y & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
@@ -308,10 +310,12 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   if (tid == 0) {
     for (int s = 0; s < NSTAGE; s++) {
       mbar_init(&full[s], NPROD);
-      mbar_init(&wfull[s], 1);
+      mbar_init(&bfull[s], 1);
       mbar_init(&empty[s], 1);
       mbar_init(&accfull[s], 1);
       mbar_init(&accempty[s], NEPI);
+      mbar_init(&wready[s], 1);
+      mbar_init(&wfree[s], NPROD);
     }
     mbar_init(fin, 1);
     *abort_flag = 0;
@@ -354,13 +358,13 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
 #pragma unroll
         for (int i = 0; i < 16; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
       }
+      const int wc = kb / WCHUNK, kin = kb % WCHUNK;
+      if (kin == 0 && !mbar_wait(&wready[wc & 1], (wc >> 1) & 1, abort_flag)) break;  // this chunk's weights
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
-      if (!mbar_wait(&wfull[s], use & 1, abort_flag)) break;  // weights of this block
       unsigned char *st = stage_base + (size_t)s * STAGE;
-      const float4 *wsm = (const float4 *)(st + WOFF);
-      const float4 w0 = wsm[2 * lane], w1 = wsm[2 * lane + 1];
-      const float x0h = ch == 0 ? w0.x : w0.z, x0l = ch == 0 ? w0.y : w0.w;
-      const float x1h = ch == 0 ? w1.x : w1.z, x1l = ch == 0 ? w1.y : w1.w;
+      // (hi, lo) of K = 2 lane and 2 lane + 1
+      const float4 wv = *(const float4 *)(wring + (size_t)(wc & 1) * WBYTES + ((size_t)kin * BK + 2 * lane) * 8);
+      const float x0h = wv.x, x0l = wv.y, x1h = wv.z, x1l = wv.w;
 #pragma unroll
       for (int i = 0; i < 16; i++) {
         const int row = r0 + i;
@@ -377,6 +381,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
+      if (kin == WCHUNK - 1 || kb == nkb - 1) mbar_arrive(&wfree[wc & 1]);  // done with this chunk's weights
 #pragma unroll
       for (int i = 0; i < 16; i++) cur[i] = nxt[i];
     }
@@ -443,7 +448,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
           const int s = kb & 1, use = kb >> 1;
-          if (!mbar_wait(&wfull[s], use & 1, abort_flag) || !mbar_wait(&full[s], use & 1, abort_flag)) {
+          if (!mbar_wait(&bfull[s], use & 1, abort_flag) || !mbar_wait(&full[s], use & 1, abort_flag)) {
             ok = false;
             break;
           }
@@ -480,30 +485,41 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       mbar_wait(fin, 0, abort_flag);
     }
   } else if (lane == 0) {
-    // ---------------- loader: B planes and the block's weights by bulk copy ----------------
+    // ---------------- loader: B planes per K block, weights per chunk, by bulk copy ----------------
     const unsigned char *bsrc = a.Bp + (size_t)tb * nkb * NP * TILE_BYTES;
-    const float4 *wsrc = a.wt + (size_t)e * a.Kp;
-    int issued = 0;
+    const float2 *wsrc = a.wt + (size_t)cidx * a.Kp;
+    const int nchunk = (nkb + WCHUNK - 1) / WCHUNK;
+    auto issue_w = [&](int c) {
+      const uint32_t bytes = (uint32_t)min(WCHUNK, nkb - c * WCHUNK) * BK * 8;
+      mbar_arrive_tx(&wready[c & 1], bytes);
+      bulk_g2s(wring + (size_t)(c & 1) * WBYTES, wsrc + (size_t)c * WCHUNK * BK, bytes, &wready[c & 1]);
+    };
+    issue_w(0);
+    if (nchunk > 1) issue_w(1);
+    int wnext = 2, issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
-      if (kb + PF_AHEAD < nkb) {
-        bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
-        bulk_prefetch_l2(wsrc + (size_t)(kb + PF_AHEAD) * BK, WBYTES);
-      }
-      mbar_arrive_tx(&wfull[s], (uint32_t)(NP * TILE_BYTES + WBYTES));
+      if (kb + PF_AHEAD < nkb) bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
+      mbar_arrive_tx(&bfull[s], (uint32_t)(NP * TILE_BYTES));
 #pragma unroll
       for (int p = 0; p < NP; p++)
-        bulk_g2s(st + BOFF + p * TILE_BYTES, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, TILE_BYTES, &wfull[s]);
-      bulk_g2s(st + WOFF, wsrc + (size_t)kb * BK, WBYTES, &wfull[s]);
+        bulk_g2s(st + BOFF + p * TILE_BYTES, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, TILE_BYTES, &bfull[s]);
       issued = kb + 1;
+      // chunk wnext reuses the slot of chunk wnext - 2 once the producers have left it
+      if (wnext < nchunk && kb >= (wnext - 1) * WCHUNK) {
+        if (!mbar_wait(&wfree[wnext & 1], ((wnext - 2) >> 1) & 1, abort_flag)) break;
+        issue_w(wnext);
+        wnext++;
+      }
     }
     // after an abort, wait (bounded) for the copies still in flight before the CTA exits
     if (*abort_flag) {
-      for (int kb = max(0, issued - NSTAGE); kb < issued; kb++) {
-        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&wfull[kb & 1], (kb >> 1) & 1); i++) __nanosleep(32);
-      }
+      for (int kb = max(0, issued - NSTAGE); kb < issued; kb++)
+        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&bfull[kb & 1], (kb >> 1) & 1); i++) __nanosleep(32);
+      for (int c = max(0, wnext - 2); c < wnext; c++)
+        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&wready[c & 1], (c >> 1) & 1); i++) __nanosleep(32);
     }
   }
   __syncwarp();
@@ -540,14 +556,15 @@ __global__ void yt_kernel(const R *__restrict__ rho, int npair, int ntk, int ng,
 }
 
 // wt[e][K] = w[(p*nen + e)*ntk + k] as float pairs: hi = float(v), lo = float(v - hi)
-__global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int nen, int Kp, float4 *__restrict__ wt) {
+__global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int nen, int Kp, float2 *__restrict__ wt) {
   const long K = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (K >= (long)npair * ntk) return;
   const int k = (int)(K / npair), p = (int)(K % npair);
   for (int e = 0; e < nen; e++) {
     double2 v = w[((size_t)p * nen + e) * ntk + k];
     const float rh = (float)v.x, ih = (float)v.y;
-    wt[(size_t)e * Kp + K] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+    wt[(size_t)(2 * e) * Kp + K] = make_float2(rh, (float)(v.x - (double)rh));
+    wt[(size_t)(2 * e + 1) * Kp + K] = make_float2(ih, (float)(v.y - (double)ih));
   }
 }
 
@@ -555,7 +572,7 @@ __device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
   atomicMax((int *)addr, __float_as_int(v));  // valid for non-negative floats
 }
 
-__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float4 *__restrict__ wt, int nen, int Kp,
+__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float2 *__restrict__ wt, int nen, int Kp,
                              long Kn, float *__restrict__ out) {
   float m = 0.f;
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nY; i += (size_t)gridDim.x * blockDim.x)
@@ -565,9 +582,8 @@ __global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const floa
   for (int e = 0; e < nen; e++) {
     float mr = 0.f, mi = 0.f;
     for (long K = (long)blockIdx.x * blockDim.x + threadIdx.x; K < Kn; K += (long)gridDim.x * blockDim.x) {
-      float4 v = wt[(size_t)e * Kp + K];
-      mr = fmaxf(mr, fabsf(v.x));
-      mi = fmaxf(mi, fabsf(v.z));
+      mr = fmaxf(mr, fabsf(wt[(size_t)(2 * e) * Kp + K].x));
+      mi = fmaxf(mi, fabsf(wt[(size_t)(2 * e + 1) * Kp + K].x));
     }
     for (int o = 16; o; o >>= 1) {
       mr = fmaxf(mr, __shfl_xor_sync(0xffffffffu, mr, o));
@@ -705,14 +721,14 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   const int Kp = (int)(((Kn + BK - 1) / BK) * BK);
   const int nplanes = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2;
   // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float4, maxes, scales, B planes
-  const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float4) * (size_t)nen * Kp;
+  const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float2) * 2 * (size_t)nen * Kp;
   const size_t mxbytes = sizeof(float) * (1 + 2 * (size_t)nen);
   const size_t sbytes = sizeof(float) * (size_t)Mp * (2 + 2 * (size_t)nen);  // rowmax, sB, sA
   const size_t bpbytes = (size_t)nplanes * 2 * Mp * Kp;
   const size_t sboff = ((ybytes + wbytes + ((mxbytes + 255) / 256) * 256 + sbytes + 1023) / 1024) * 1024;
   unsigned char *base = (unsigned char *)grow(ws.planes, ws.planes_bytes, sboff + bpbytes + 1024);
   float *Yt = (float *)base;
-  float4 *wt = (float4 *)(base + ybytes);
+  float2 *wt = (float2 *)(base + ybytes);
   float *maxes = (float *)(base + ybytes + wbytes);
   float *rowmax = (float *)(base + ybytes + wbytes + ((mxbytes + 255) / 256) * 256);
   float *sBv = rowmax + Mp, *sAv = sBv + Mp;
@@ -767,7 +783,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
   // per stage: A planes, B planes, the block's weights; then the barriers
-  const size_t smem = 1024 + (size_t)NSTAGE * (2 * (size_t)nplanes * TILE_BYTES + WBYTES) + 128 + sizeof(float) * BM;
+  const size_t smem = 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes * TILE_BYTES + 2 * (size_t)WBYTES + 256 + sizeof(float) * BM;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
   void (*kern)(TcArgs);
   if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, true, false>;
