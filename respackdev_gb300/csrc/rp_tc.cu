@@ -301,8 +301,9 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
   float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int e = blockIdx.y >> 1, ch = blockIdx.y & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
-  const int2 tt = a.tiles[blockIdx.x];
+  // channels vary fastest, so the CTAs running together share their operand rows in L2
+  const int e = blockIdx.x >> 1, ch = blockIdx.x & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
+  const int2 tt = a.tiles[blockIdx.y];
   const int ta = tt.x, tb = tt.y;
   const int nkb = a.Kp / BK;
   const int nsub = (nkb + a.ksub_blocks - 1) / a.ksub_blocks;
@@ -790,7 +791,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   else if (precision == RP_PREC_BF16X3) kern = tc_gram_kernel<3, true, true>;
   else kern = tc_gram_kernel<2, false, false>;
   RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)tl.size(), 2 * nen);
+  dim3 grid(2 * nen, (unsigned)tl.size());
   RP_CUDA(cudaEventRecord(ws.ev0, st));
   kern<<<grid, NTHREADS, smem, st>>>(a);
   RP_CUDA(cudaEventRecord(ws.ev1, st));
