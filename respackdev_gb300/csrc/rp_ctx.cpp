@@ -230,9 +230,9 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   int jmax = 8;
   const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];
   auto smem_of = [&](int j, size_t elt) {
-    int D1 = 2 * ep[0] + 1 <= n1 ? 2 * ep[0] + 1 : n1, D2 = 2 * ep[1] + 1 <= n2 ? 2 * ep[1] + 1 : n2;
-    return elt * ((size_t)n1 + n2 + n3 + 2 * (size_t)n1 * n2 + (size_t)D1 * n2 + D1 * D2 + (size_t)j * ng) +
-           sizeof(int) * ((size_t)D1 + D2 + ng);
+    rp::PairGeom gq;
+    gq.n1 = n1; gq.n2 = n2; gq.n3 = n3; gq.R1 = ep[0]; gq.R2 = ep[1]; gq.ng = ng;
+    return rp::pair_density_smem(gq, j, elt == sizeof(double) * 2);
   };
   const size_t elt = (fast && !S.params.pair_fp64) ? sizeof(float) * 2 : sizeof(double) * 2;
   while (jmax > 1 && smem_of(jmax, elt) > 220 * 1024) jmax--;

@@ -72,6 +72,8 @@ struct PairGeom {
 // out64: rho[(pair*ntk + k)*ng + g] (double2, FP32-rounded values, plain path)
 int launch_pair_density_fp64(const float2 *ur, const PairGeom &g, const PairChunks &c, double2 *out,
                              cudaStream_t st);
+// shared memory of a pair-density CTA holding jmax pairs (callers size their chunks by it)
+size_t pair_density_smem(const PairGeom &g, int jmax, bool fp64);
 // FP32 path; writes the same layout in float2
 int launch_pair_density_fp32(const float2 *ur, const PairGeom &g, const PairChunks &c, float2 *out,
                              cudaStream_t st);

@@ -456,9 +456,9 @@ static void int_q_rho(rp_int *c, int iq, const std::vector<int> &pv, const std::
   // pairs grouped by virtual function, as many per CTA as shared memory allows
   const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];
   auto smem_of = [&](int j) {
-    const int D1 = 2 * ext[0] + 1 <= n1 ? 2 * ext[0] + 1 : n1, D2 = 2 * ext[1] + 1 <= n2 ? 2 * ext[1] + 1 : n2;
-    return sizeof(float2) * ((size_t)n1 + n2 + n3 + 2 * (size_t)n1 * n2 + (size_t)D1 * n2 + D1 * D2 + (size_t)j * ngp) +
-           sizeof(int) * ((size_t)D1 + D2 + ngp);
+    rp::PairGeom gq;
+    gq.n1 = n1; gq.n2 = n2; gq.n3 = n3; gq.R1 = ext[0]; gq.R2 = ext[1]; gq.ng = ngp;
+    return rp::pair_density_smem(gq, j, false);
   };
   int jmax = 8;
   while (jmax > 1 && smem_of(jmax) > 220 * 1024) jmax--;

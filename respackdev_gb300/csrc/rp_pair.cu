@@ -49,7 +49,9 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
   const int kq = a.kpq[k];
   const int s1 = a.shift[3 * k], s2 = a.shift[3 * k + 1], s3 = a.shift[3 * k + 2];
   const int vir = a.chunk_vir[ch], first = a.chunk_first[ch], cnt = a.chunk_count[ch];
-  T2 *tw1 = (T2 *)smem, *tw2 = tw1 + n1, *tw3 = tw2 + n2;
+  // twiddle tables TW1[x][c1] = e^{-2 pi i f1(c1) x / n1}, TW2[y][c2] likewise: the
+  // lanes of a warp read consecutive entries, and no index arithmetic per term
+  T2 *TW1 = (T2 *)smem, *TW2 = TW1 + (size_t)n1 * D1, *tw3 = TW2 + (size_t)n2 * D2;
   T2 *ui = tw3 + n3;              // n12
   T2 *P = ui + n12;               // n12
   T2 *X = P + n12;                // D1*n2
@@ -57,11 +59,12 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
   T2 *acc = Y + D1 * D2;          // jmax*ng
   int *f1 = (int *)(acc + (size_t)a.jmax * ng), *f2 = f1 + D1;
   int *gsel = f2 + D2;            // ng: c1 | c2 << 10 | f3 << 20
-  for (int j = tid; j < n1; j += nt) tw1[j] = ToT2<T>::tw(j, n1);
-  for (int j = tid; j < n2; j += nt) tw2[j] = ToT2<T>::tw(j, n2);
   for (int j = tid; j < n3; j += nt) tw3[j] = ToT2<T>::tw(j, n3);
   for (int j = tid; j < D1; j += nt) f1[j] = c1 ? modp2(-(j - a.R1) - s1, n1) : j;
   for (int j = tid; j < D2; j += nt) f2[j] = c2 ? modp2(-(j - a.R2) - s2, n2) : j;
+  __syncthreads();
+  for (int i = tid; i < n1 * D1; i += nt) { const int x = i / D1, c = i % D1; TW1[i] = ToT2<T>::tw((f1[c] * x) % n1, n1); }
+  for (int i = tid; i < n2 * D2; i += nt) { const int y = i / D2, c = i % D2; TW2[i] = ToT2<T>::tw((f2[c] * y) % n2, n2); }
   for (int g = tid; g < ng; g += nt) {
     const int *l = a.lg0 + 3 * g;
     int i1 = c1 ? l[0] + a.R1 : modp2(-l[0] - s1, n1);
@@ -80,28 +83,32 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
       const float2 *uj_g = ur + ((size_t)k * a.ncb + occ) * (size_t)n12 * n3 + (size_t)z * n12;
       for (int i = tid; i < n12; i += nt) P[i] = cmul(cconj(ui[i]), ToT2<T>::cvt(uj_g[i]));
       __syncthreads();
-      // x pass: X[c1,y] = sum_x P[x,y] e^{-2 pi i f1 x/n1}
-      for (int o = tid; o < D1 * n2; o += nt) {
-        const int cc = o % D1, y = o / D1, f = f1[cc];
-        T2 s = mk<T>(0, 0);
-        int idx = 0;
+      // x pass: X[c1,y] = sum_x P[x,y] TW1[x][c1], two c1 (cc, cc + H1) per thread
+      const int H1 = (D1 + 1) / 2, H2 = (D2 + 1) / 2;
+      for (int o = tid; o < H1 * n2; o += nt) {
+        const int cc = o % H1, y = o / H1, cb = min(cc + H1, D1 - 1);
+        T2 sa = mk<T>(0, 0), sb = mk<T>(0, 0);
+        const T2 *pr = P + (size_t)n1 * y;
         for (int x = 0; x < n1; x++) {
-          cfma(s, P[x + n1 * y], tw1[idx]);
-          idx += f; if (idx >= n1) idx -= n1;
+          const T2 pv = pr[x];
+          cfma(sa, pv, TW1[(size_t)x * D1 + cc]);
+          cfma(sb, pv, TW1[(size_t)x * D1 + cb]);
         }
-        X[o] = s;
+        X[cc + D1 * y] = sa;
+        if (cc + H1 < D1) X[cc + H1 + D1 * y] = sb;
       }
       __syncthreads();
-      // y pass: Y[c1,c2] = sum_y X[c1,y] e^{-2 pi i f2 y/n2}
-      for (int o = tid; o < D1 * D2; o += nt) {
-        const int cc1 = o % D1, cc2 = o / D1, f = f2[cc2];
-        T2 s = mk<T>(0, 0);
-        int idx = 0;
+      // y pass: Y[c1,c2] = sum_y X[c1,y] TW2[y][c2], two c2 (c, c + H2) per thread
+      for (int o = tid; o < D1 * H2; o += nt) {
+        const int cc1 = o % D1, cc2 = o / D1, cb = min(cc2 + H2, D2 - 1);
+        T2 sa = mk<T>(0, 0), sb = mk<T>(0, 0);
         for (int y = 0; y < n2; y++) {
-          cfma(s, X[cc1 + D1 * y], tw2[idx]);
-          idx += f; if (idx >= n2) idx -= n2;
+          const T2 xv = X[cc1 + D1 * y];
+          cfma(sa, xv, TW2[(size_t)y * D2 + cc2]);
+          cfma(sb, xv, TW2[(size_t)y * D2 + cb]);
         }
-        Y[o] = s;
+        Y[cc1 + D1 * cc2] = sa;
+        if (cc2 + H2 < D2) Y[cc1 + D1 * (cc2 + H2)] = sb;
       }
       __syncthreads();
       // z term of each G
@@ -126,16 +133,21 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
   }
 }
 
+size_t pair_density_smem(const PairGeom &g, int jmax, bool fp64) {
+  const int D1 = 2 * g.R1 + 1 <= g.n1 ? 2 * g.R1 + 1 : g.n1, D2 = 2 * g.R2 + 1 <= g.n2 ? 2 * g.R2 + 1 : g.n2;
+  const size_t elt = fp64 ? sizeof(double2) : sizeof(float2);
+  return elt * ((size_t)g.n1 * D1 + (size_t)g.n2 * D2 + g.n3 + 2 * (size_t)g.n1 * g.n2 + (size_t)D1 * g.n2 +
+                (size_t)D1 * D2 + (size_t)jmax * g.ng) +
+         sizeof(int) * ((size_t)D1 + D2 + g.ng);
+}
+
 template <typename T>
 static int launch_pd(const float2 *ur, const PairGeom &g, const PairChunks &c, typename C2<T>::t *out,
                      cudaStream_t st) {
   using T2 = typename C2<T>::t;
   if (c.nchunk == 0) return 0;
-  const int D1 = 2 * g.R1 + 1 <= g.n1 ? 2 * g.R1 + 1 : g.n1, D2 = 2 * g.R2 + 1 <= g.n2 ? 2 * g.R2 + 1 : g.n2;
   if (g.n1 > 1023 || g.n2 > 1023 || g.n3 > 1023) fail(1, "FFT box dimension above 1023");
-  size_t smem = sizeof(T2) * ((size_t)g.n1 + g.n2 + g.n3 + 2 * (size_t)g.n1 * g.n2 + (size_t)D1 * g.n2 + D1 * D2 +
-                              (size_t)c.jmax * g.ng) +
-                sizeof(int) * ((size_t)D1 + D2 + g.ng);
+  const size_t smem = pair_density_smem(g, c.jmax, sizeof(T2) == sizeof(double2));
   if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
   RP_CUDA(cudaFuncSetAttribute(pair_density_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   PairArgs a;
