@@ -21,15 +21,15 @@
 // smaller, go to a second accumulator.  After each sub-chunk the epilogue
 // warps add both, times the rows' scales, into an FP64 copy of the tile.
 //
-// Kernel layout: one CTA per (upper tile, frequency, Re/Im weight), 448 threads.
-//   warps 0-7   producers: read the FP32 rows of the A operand (prefetched one K
+// Kernel layout: one CTA per (upper tile, frequency, Re/Im weight), 704 threads.
+//   warps 0-15  producers (8 rows each): read the FP32 rows of the A operand (prefetched one K
 //               block ahead in registers), multiply by the weights, split into
 //               planes and store them into shared memory in the 128-byte-swizzled
 //               K-major layout the tensor core reads;
-//   warps 8-11  epilogue: drain the FP32 accumulators from tensor memory
+//   warps 16-19 epilogue: drain the FP32 accumulators from tensor memory
 //               (tcgen05.ld) into a float-pair running sum, then the FP64 tile;
-//   warp 12     allocates tensor memory and issues tcgen05.mma (one thread);
-//   warp 13     loader (one thread): bulk-copies (cp.async.bulk) the B operand
+//   warp 20     allocates tensor memory and issues tcgen05.mma (one thread);
+//   warp 21     loader (one thread): bulk-copies (cp.async.bulk) the B operand
 //               planes -- split once per batch by bplanes_kernel and shared by
 //               every channel -- and the block's weights into the stage.
 // Two operand stages overlap loading, production and MMA.  Every mbarrier wait
@@ -54,7 +54,8 @@ constexpr int BN = 128;          // tile columns (b)
 constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
 constexpr int NSTAGE = 2;
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
-constexpr int NPROD = 256, NEPI = 128;    // 8 producer warps, 4 epilogue warps, MMA warp, loader warp
+constexpr int NPROD = 512, NEPI = 128;    // 16 producer warps, 4 epilogue warps, MMA warp, loader warp
+constexpr int PROWS = BM / (NPROD / 32); // A rows per producer warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
 constexpr int WCHUNK = 16;                 // K blocks per weight chunk
@@ -285,7 +286,8 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // NP operand planes, EXACT integer leading plane, BF16 or FP16.  One CTA per
 // (upper tile, frequency, Re/Im weight); see the file comment for the roles.
 template <int NP, bool EXACT, bool BF16>
-__global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
+// 22 warps: at most 6 on one SM sub-partition, whose 16K registers allow 85 per thread
+__global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
@@ -337,27 +339,27 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
 
   if (warp < NPROD / 32) {
     // ---------------- producers: the weighted A operand ----------------
-    // warp pw owns rows 16 pw .. 16 pw + 15; lane l the K pair 2l, 2l+1 of every
+    // warp pw owns rows PROWS pw .. PROWS (pw + 1) - 1; lane l the K pair 2l, 2l+1 of every
     // block, so the global reads are coalesced (one 256-byte row per instruction),
-    // the lane's two weights serve all 16 rows, and each plane store writes one
+    // the lane's two weights serve all the warp's rows, and each plane store writes one
     // full 128-byte swizzled row.
-    const int pw = warp, r0 = 16 * pw;
+    const int pw = warp, r0 = PROWS * pw;
     const float2 *ya = (const float2 *)(a.Yt + (size_t)(ta * BM + r0) * a.Kp) + lane;
     const size_t rstride = (size_t)a.Kp / 2;  // float2 per row
-    float2 cur[16], nxt[16];
+    float2 cur[PROWS], nxt[PROWS];
 #pragma unroll
-    for (int i = 0; i < 16; i++) cur[i] = __ldg(ya + i * rstride);
+    for (int i = 0; i < PROWS; i++) cur[i] = __ldg(ya + i * rstride);
     const uint32_t cofs = (uint32_t)(lane & 3) * 4, chunk = (uint32_t)(lane >> 2);
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
       if (kb + 1 < nkb) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
+        for (int i = 0; i < PROWS; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
       }
       // DRAM -> L2 a few blocks ahead, one line per lane group: lanes 0 and 16 cover a row's 256 bytes
       if (kb + PF_AHEAD < nkb && (lane & 15) == 0) {
 #pragma unroll
-        for (int i = 0; i < 16; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
+        for (int i = 0; i < PROWS; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
       }
       const int wc = kb / WCHUNK, kin = kb % WCHUNK;
       if (kin == 0 && !mbar_wait(&wready[wc & 1], (wc >> 1) & 1, abort_flag)) break;  // this chunk's weights
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       const float4 wv = *(const float4 *)(wring + (size_t)(wc & 1) * WBYTES + ((size_t)kin * BK + 2 * lane) * 8);
       const float x0h = wv.x, x0l = wv.y, x1h = wv.z, x1l = wv.w;
 #pragma unroll
-      for (int i = 0; i < 16; i++) {
+      for (int i = 0; i < PROWS; i++) {
         const int row = r0 + i;
         // (wh + wl) * y * s as a float pair: rounded head product plus its exact remainder
         const float sa = sA_s[r0 + i];
@@ -384,7 +386,7 @@ __global__ void __launch_bounds__(NTHREADS, 1) tc_gram_kernel(TcArgs a) {
       mbar_arrive(&full[s]);
       if (kin == WCHUNK - 1 || kb == nkb - 1) mbar_arrive(&wfree[wc & 1]);  // done with this chunk's weights
 #pragma unroll
-      for (int i = 0; i < 16; i++) cur[i] = nxt[i];
+      for (int i = 0; i < PROWS; i++) cur[i] = nxt[i];
     }
   } else if (warp < MMA_WARP) {
     // ---------------- epilogue: fold each sub-chunk into a float-pair accumulator ----------------
