@@ -13,6 +13,12 @@
 // the sphere), a y pass (only its (x,y) frequency pairs), then each G's z term
 // is accumulated.  One CTA owns one k and up to JMAX pairs that share the same
 // virtual band, so u_{i,k+q} is read from HBM once per slab and reused.
+//
+// Two kernels: pair_density_kernel (FP64 arithmetic, the plain path: x pass,
+// y pass, z term) and pair_slab_kernel (FP32, the fast path), which runs the y
+// pass first with the lanes along x so that every thread streams its own
+// column of the product straight from global memory and keeps two pairs and up
+// to 16 output frequencies in registers.
 #include "rp_dev.cuh"
 #include "rp_host.h"
 
@@ -28,10 +34,6 @@ struct PairArgs {
 };
 
 template <typename T> struct ToT2;
-template <> struct ToT2<float> {
-  __device__ static float2 cvt(float2 v) { return v; }
-  __device__ static float2 tw(int j, int n) { float s, c; sincospif(-2.0f * j / n, &s, &c); return make_float2(c, s); }
-};
 template <> struct ToT2<double> {
   __device__ static double2 cvt(float2 v) { return make_double2(v.x, v.y); }
   __device__ static double2 tw(int j, int n) { double s, c; sincospi(-2.0 * j / n, &s, &c); return make_double2(c, s); }
@@ -133,41 +135,291 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 path.  One CTA per (chunk of <= jmax pairs sharing a virtual band, k);
+// the chunks of one k are consecutive in the grid, so the occupied bands of k
+// stay in L2 while every virtual band is read from HBM once.  Per z slab:
+//   pass 1 (y):  X[q][x][c2] = sum_y P_{2q}[x,y] TW2[y][c2], and the same for
+//                pair 2q+1 in the other half of the float4.  Thread (q, x)
+//                loads conj(u_vir) and both u_occ of its column from global
+//                memory (32 lanes = 32 consecutive x: coalesced) and keeps
+//                2 pairs x 16 frequencies in registers; the twiddle rows are
+//                warp-uniform (broadcast) 16-byte loads.
+//   pass 2 (x):  Y[j][c2][c1] = sum_x X[j][x][c2] TW1[x][c1], thread
+//                (q, tile) with a tile = (c2, group of 4 c1) holding at least
+//                one G of the sphere (about 30 of the 52 tiles of a 13x13
+//                square); both pairs of the couple per load.
+//   z term:      acc[j][g] += Y[j][c2(g)][c1(g)] e^{-2 pi i f3(g) z / n3}.
+constexpr int PD_THREADS = 160;
+constexpr int PD_CGMAX = 16;  // pass-1 output frequencies per register group, at most
+
+// pass-1 register group for D2 output frequencies: an even count (the twiddles
+// are read in 16-byte pairs) from a few compiled widths
+__host__ __device__ inline int pd_group(int D2) {
+  const int need = (D2 + 1) & ~1;
+  return need <= 8 ? 8 : need <= 12 ? 12 : need <= 14 ? 14 : 16;
+}
+
+struct PdLayout {
+  int D1, D2, D1P, D2P, D2X, SQ, nq, ntl;
+  size_t oTW1, oTZ, oX, oY, oAcc, oSel, oF, oTile, total;
+};
+
+__host__ __device__ inline size_t pd_up16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+// Shared-memory carve-up of pair_slab_kernel (host and device agree on it).
+//   TW2 [n2][D2P] float2, zero beyond D2      TW1 [n1][D1P] float2, zero beyond D1
+//   TZ  [2][n3]  float2 (z twiddles of the slab, double-buffered by slab parity)
+//   X   [nq][SQ] float4: row x at x*D2X, column c2 -> (pair 2q, pair 2q+1)
+//   Y   [jmax][D2][D1] float2        acc [jmax][ng] float2
+//   sel [ng] int: c1 | c2 << 10 | f3 << 20          f1 [D1], f2 [D2] int
+//   tile flags [ntl] and tile list [ntl + 1] int, ntl = (D1P / 4) D2, tile = grp D2 + c2
+// D2X is odd and SQ = D2X (mod 8), so the 16-byte column stores of pass 1 and
+// the (q, c2)-consecutive loads of pass 2 hit distinct bank quads.
+__host__ __device__ inline PdLayout pd_layout(int n1, int n2, int n3, int R1, int R2, int ng, int jmax) {
+  PdLayout L;
+  L.D1 = 2 * R1 + 1 <= n1 ? 2 * R1 + 1 : n1;
+  L.D2 = 2 * R2 + 1 <= n2 ? 2 * R2 + 1 : n2;
+  const int cg = pd_group(L.D2);
+  L.D2P = (L.D2 + cg - 1) / cg * cg;
+  L.D1P = (L.D1 + 3) / 4 * 4;
+  L.D2X = L.D2 | 1;
+  L.nq = (jmax + 1) / 2;
+  int sq = n1 * L.D2X;
+  while ((sq - L.D2X) % 8) sq++;
+  L.SQ = sq;
+  size_t o = pd_up16(sizeof(float2) * (size_t)n2 * L.D2P);
+  L.oTW1 = o; o += pd_up16(sizeof(float2) * (size_t)n1 * L.D1P);
+  L.oTZ = o;  o += pd_up16(sizeof(float2) * 2 * (size_t)n3);
+  L.oX = o;   o += sizeof(float4) * (size_t)L.nq * L.SQ;
+  L.oY = o;   o += pd_up16(sizeof(float2) * (size_t)jmax * L.D1 * L.D2);
+  L.oAcc = o; o += pd_up16(sizeof(float2) * (size_t)jmax * ng);
+  L.oSel = o; o += pd_up16(sizeof(int) * (size_t)ng);
+  L.oF = o;   o += pd_up16(sizeof(int) * (size_t)(L.D1 + L.D2));
+  L.ntl = (L.D1P / 4) * L.D2;
+  L.oTile = o; o += sizeof(int) * (2 * (size_t)L.ntl + 1);
+  L.total = o;
+  return L;
+}
+
+__device__ __forceinline__ float2 tw32(int j, int n) {
+  float s, c;
+  sincospif(-2.0f * j / n, &s, &c);
+  return make_float2(c, s);
+}
+// conj(a) * b
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.x, b.y, -a.y * b.x));
+}
+
+template <int CG>
+__global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *__restrict__ ur, PairArgs a,
+                                                                   float2 *__restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ch = blockIdx.x, k = blockIdx.y, tid = threadIdx.x;
+  const int n1 = a.n1, n2 = a.n2, n3 = a.n3, n12 = n1 * n2, ng = a.ng;
+  const PdLayout L = pd_layout(n1, n2, n3, a.R1, a.R2, ng, a.jmax);
+  const int D1 = L.D1, D2 = L.D2;
+  const bool c1 = 2 * a.R1 + 1 <= n1, c2 = 2 * a.R2 + 1 <= n2;
+  const int kq = a.kpq[k];
+  const int s1 = a.shift[3 * k], s2 = a.shift[3 * k + 1], s3 = a.shift[3 * k + 2];
+  const int vir = a.chunk_vir[ch], first = a.chunk_first[ch], cnt = a.chunk_count[ch];
+  const int nq = (cnt + 1) / 2;
+  float2 *TW2 = (float2 *)smem, *TW1 = (float2 *)(smem + L.oTW1), *TZ = (float2 *)(smem + L.oTZ);
+  float4 *X = (float4 *)(smem + L.oX);
+  float2 *Y = (float2 *)(smem + L.oY), *acc = (float2 *)(smem + L.oAcc);
+  int *gsel = (int *)(smem + L.oSel), *f1 = (int *)(smem + L.oF), *f2 = f1 + D1;
+  int *tflag = (int *)(smem + L.oTile), *tlist = tflag + L.ntl;  // tlist[0] = count
+  for (int i = tid; i < L.ntl; i += PD_THREADS) tflag[i] = 0;
+  for (int j = tid; j < D1; j += PD_THREADS) f1[j] = c1 ? modp2(-(j - a.R1) - s1, n1) : j;
+  for (int j = tid; j < D2; j += PD_THREADS) f2[j] = c2 ? modp2(-(j - a.R2) - s2, n2) : j;
+  __syncthreads();
+  for (int i = tid; i < n2 * L.D2P; i += PD_THREADS) {
+    const int y = i / L.D2P, c = i % L.D2P;
+    TW2[i] = c < D2 ? tw32((f2[c] * y) % n2, n2) : make_float2(0.f, 0.f);
+  }
+  for (int i = tid; i < n1 * L.D1P; i += PD_THREADS) {
+    const int x = i / L.D1P, c = i % L.D1P;
+    TW1[i] = c < D1 ? tw32((f1[c] * x) % n1, n1) : make_float2(0.f, 0.f);
+  }
+  for (int g = tid; g < ng; g += PD_THREADS) {
+    const int *l = a.lg0 + 3 * g;
+    const int i1 = c1 ? l[0] + a.R1 : modp2(-l[0] - s1, n1);
+    const int i2 = c2 ? l[1] + a.R2 : modp2(-l[1] - s2, n2);
+    const int i3 = modp2(-l[2] - s3, n3);
+    gsel[g] = i1 | (i2 << 10) | (i3 << 20);
+    tflag[(i1 >> 2) * D2 + i2] = 1;
+  }
+  for (int i = tid; i < cnt * ng; i += PD_THREADS) acc[i] = make_float2(0.f, 0.f);
+  __syncthreads();
+  if (tid < 32) {  // compact the flagged tiles in (group, c2) order; read after pass 1's barrier
+    int n = 0;
+    for (int b = 0; b < L.ntl; b += 32) {
+      const bool f = b + tid < L.ntl && tflag[b + tid];
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (f) tlist[1 + n + __popc(m & ((1u << tid) - 1u))] = b + tid;
+      n += __popc(m);
+    }
+    if (tid == 0) tlist[0] = n;
+  }
+  const size_t bstride = (size_t)n12 * n3;
+  const float2 *uvir = ur + ((size_t)kq * a.ncb + vir) * bstride, *uocc = ur + (size_t)k * a.ncb * bstride;
+  for (int z = 0; z < n3; z++) {
+    float2 *tz = TZ + (z & 1) * n3;
+    for (int i = tid; i < n3; i += PD_THREADS) tz[i] = tw32((i * z) % n3, n3);
+    // pass 1: row = (couple q1, column x1); one row per thread when nq n1 <= PD_THREADS
+    for (int row = tid; row < nq * n1; row += PD_THREADS) {
+      const int q1 = row / n1, x1 = row - q1 * n1;
+      const int jA = 2 * q1, jB = min(2 * q1 + 1, cnt - 1);
+      const float2 *pv = uvir + x1;
+      const float2 *pa = uocc + (size_t)a.pair_occ[a.pair_list[first + jA]] * bstride + x1;
+      const float2 *pb = uocc + (size_t)a.pair_occ[a.pair_list[first + jB]] * bstride + x1;
+      const size_t zo = (size_t)z * n12;
+      for (int cg = 0; cg < D2; cg += CG) {
+        float2 sa[CG], sb[CG];
+#pragma unroll
+        for (int c = 0; c < CG; c++) { sa[c] = make_float2(0.f, 0.f); sb[c] = sa[c]; }
+        const float4 *twr = (const float4 *)(TW2 + cg);
+        auto step = [&](float2 v, float2 va, float2 vb, int y) {
+          const float2 PA = cmulc(v, va), PB = cmulc(v, vb);
+          const float4 *t = twr + (size_t)y * (L.D2P / 2);
+#pragma unroll
+          for (int c = 0; c < CG / 2; c++) {
+            const float4 w = t[c];
+            const float2 w0 = make_float2(w.x, w.y), w1 = make_float2(w.z, w.w);
+            cfma(sa[2 * c], PA, w0); cfma(sb[2 * c], PB, w0);
+            cfma(sa[2 * c + 1], PA, w1); cfma(sb[2 * c + 1], PB, w1);
+          }
+        };
+        // four rows in flight: each row's registers are refilled with the row
+        // four ahead as soon as they are consumed (row index clamped to the
+        // slab, so the loads need no guard)
+        const int n2f = n2 & ~3;
+        float2 nv[4], na[4], nb[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const size_t o = zo + (size_t)min(u, n2 - 1) * n1;
+          nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
+        }
+        for (int y0 = 0; y0 < n2f; y0 += 4) {
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const float2 cv = nv[u], ca = na[u], cb = nb[u];
+            const size_t o = zo + (size_t)min(y0 + 4 + u, n2 - 1) * n1;
+            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
+            step(cv, ca, cb, y0 + u);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 3; u++)
+          if (n2f + u < n2) step(nv[u], na[u], nb[u], n2f + u);
+        float4 *xr = X + (size_t)q1 * L.SQ + (size_t)x1 * L.D2X + cg;
+#pragma unroll
+        for (int c = 0; c < CG; c++)
+          if (cg + c < D2) xr[c] = make_float4(sa[c].x, sa[c].y, sb[c].x, sb[c].y);
+      }
+    }
+    __syncthreads();
+    // pass 2: item = (q, tile)
+    const int ntile = tlist[0];
+    for (int it = tid; it < ntile * nq; it += PD_THREADS) {
+      const int q = it / ntile, t = tlist[1 + it - q * ntile], grp = t / D2, cc2 = t - grp * D2;
+      float2 ya[4], yb[4];
+#pragma unroll
+      for (int c = 0; c < 4; c++) { ya[c] = make_float2(0.f, 0.f); yb[c] = ya[c]; }
+      const float4 *xc = X + (size_t)q * L.SQ + cc2;
+      const float4 *tw = (const float4 *)(TW1 + 4 * grp);
+#pragma unroll 4
+      for (int x = 0; x < n1; x++) {
+        const float4 v = xc[(size_t)x * L.D2X];
+        const float2 va = make_float2(v.x, v.y), vb = make_float2(v.z, v.w);
+        const float4 t0 = tw[(size_t)x * (L.D1P / 2)], t1 = tw[(size_t)x * (L.D1P / 2) + 1];
+        const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
+                             make_float2(t1.z, t1.w)};
+#pragma unroll
+        for (int c = 0; c < 4; c++) { cfma(ya[c], va, w[c]); cfma(yb[c], vb, w[c]); }
+      }
+      float2 *yA = Y + (size_t)(2 * q) * D1 * D2 + (size_t)cc2 * D1 + 4 * grp;
+      const bool hasB = 2 * q + 1 < cnt;
+#pragma unroll
+      for (int c = 0; c < 4; c++)
+        if (4 * grp + c < D1) {
+          yA[c] = ya[c];
+          if (hasB) yA[(size_t)D1 * D2 + c] = yb[c];
+        }
+    }
+    __syncthreads();
+    // z term (overlaps the next slab's pass 1, which touches neither Y nor this tz)
+    for (int g = tid; g < ng; g += PD_THREADS) {
+      const int sel = gsel[g];
+      const int yi = (sel & 1023) + D1 * ((sel >> 10) & 1023);
+      const float2 t = tz[sel >> 20];
+      for (int j = 0; j < cnt; j++) cfma(acc[(size_t)j * ng + g], Y[(size_t)j * D1 * D2 + yi], t);
+    }
+  }
+  __syncthreads();
+  const float inv = (float)(1.0 / ((double)n12 * n3));
+  for (int jj = 0; jj < cnt; jj++) {
+    const int p = a.pair_list[first + jj];
+    float2 *dst = out + ((size_t)p * a.ntk + k) * ng;
+    for (int g = tid; g < ng; g += PD_THREADS) {
+      const float2 v = acc[(size_t)jj * ng + g];
+      dst[g] = make_float2(v.x * inv, v.y * inv);
+    }
+  }
+}
+
 size_t pair_density_smem(const PairGeom &g, int jmax, bool fp64) {
+  if (!fp64) return pd_layout(g.n1, g.n2, g.n3, g.R1, g.R2, g.ng, jmax).total;
   const int D1 = 2 * g.R1 + 1 <= g.n1 ? 2 * g.R1 + 1 : g.n1, D2 = 2 * g.R2 + 1 <= g.n2 ? 2 * g.R2 + 1 : g.n2;
-  const size_t elt = fp64 ? sizeof(double2) : sizeof(float2);
+  const size_t elt = sizeof(double2);
   return elt * ((size_t)g.n1 * D1 + (size_t)g.n2 * D2 + g.n3 + 2 * (size_t)g.n1 * g.n2 + (size_t)D1 * g.n2 +
                 (size_t)D1 * D2 + (size_t)jmax * g.ng) +
          sizeof(int) * ((size_t)D1 + D2 + g.ng);
 }
 
-template <typename T>
-static int launch_pd(const float2 *ur, const PairGeom &g, const PairChunks &c, typename C2<T>::t *out,
-                     cudaStream_t st) {
-  using T2 = typename C2<T>::t;
-  if (c.nchunk == 0) return 0;
-  if (g.n1 > 1023 || g.n2 > 1023 || g.n3 > 1023) fail(1, "FFT box dimension above 1023");
-  const size_t smem = pair_density_smem(g, c.jmax, sizeof(T2) == sizeof(double2));
-  if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
-  RP_CUDA(cudaFuncSetAttribute(pair_density_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+static PairArgs pair_args(const PairGeom &g, const PairChunks &c) {
   PairArgs a;
   a.ntk = g.ntk; a.ncb = g.ncb; a.n1 = g.n1; a.n2 = g.n2; a.n3 = g.n3; a.ng = g.ng; a.R1 = g.R1; a.R2 = g.R2;
   a.kpq = g.kpq; a.shift = g.shift; a.lg0 = g.lg0;
   a.chunk_vir = c.chunk_vir; a.chunk_first = c.chunk_first; a.chunk_count = c.chunk_count;
   a.pair_list = c.pair_list; a.pair_occ = c.pair_occ; a.jmax = c.jmax;
-  dim3 grid(g.ntk, c.nchunk);
-  pair_density_kernel<T><<<grid, 256, smem, st>>>(ur, a, out);
-  RP_CUDA(cudaGetLastError());
-  return 1;
+  return a;
 }
 
 int launch_pair_density_fp64(const float2 *ur, const PairGeom &g, const PairChunks &c, double2 *out,
                              cudaStream_t st) {
-  return launch_pd<double>(ur, g, c, out, st);
+  if (c.nchunk == 0) return 0;
+  if (g.n1 > 1023 || g.n2 > 1023 || g.n3 > 1023) fail(1, "FFT box dimension above 1023");
+  const size_t smem = pair_density_smem(g, c.jmax, true);
+  if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
+  RP_CUDA(cudaFuncSetAttribute(pair_density_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(g.ntk, c.nchunk);
+  pair_density_kernel<double><<<grid, 256, smem, st>>>(ur, pair_args(g, c), out);
+  RP_CUDA(cudaGetLastError());
+  return 1;
 }
+
 int launch_pair_density_fp32(const float2 *ur, const PairGeom &g, const PairChunks &c, float2 *out,
                              cudaStream_t st) {
-  return launch_pd<float>(ur, g, c, out, st);
+  if (c.nchunk == 0) return 0;
+  if (g.n1 > 1023 || g.n2 > 1023 || g.n3 > 1023) fail(1, "FFT box dimension above 1023");
+  if (g.ntk > 65535) fail(1, "more than 65535 k points in one pair-density launch");
+  const size_t smem = pair_density_smem(g, c.jmax, false);
+  if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
+  const int D2 = 2 * g.R2 + 1 <= g.n2 ? 2 * g.R2 + 1 : g.n2;
+  auto kern = pair_slab_kernel<16>;
+  switch (pd_group(D2)) {
+    case 8: kern = pair_slab_kernel<8>; break;
+    case 12: kern = pair_slab_kernel<12>; break;
+    case 14: kern = pair_slab_kernel<14>; break;
+    default: break;
+  }
+  RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid(c.nchunk, g.ntk);
+  kern<<<grid, PD_THREADS, smem, st>>>(ur, pair_args(g, c), out);
+  RP_CUDA(cudaGetLastError());
+  return 1;
 }
 
 // ---------------------------------------------------------------------------
