@@ -9,7 +9,8 @@
 // (frequency, direction) matrix is inverted by Gauss-Jordan elimination with
 // partial pivoting on |re|+|im| (izamax's norm), one kernel pair per pivot
 // column over all matrices at once, and the row/column permutation undone at
-// the end.
+// the end.  The select kernel scales the pivot column by the pivot's
+// reciprocal once, so the update is four FP64 FMAs per element.
 #include "rp_dev.cuh"
 #include "rp_host.h"
 
@@ -100,16 +101,21 @@ __global__ void gj_select_kernel(double2 *__restrict__ A, int n, int k, double2 
   }
   // NaN entries never win the comparison: fall back to row k's slot and flag
   const int p = (si[0] >= 0 && si[0] < n) ? si[0] : k;
+  __shared__ double2 sd;
   if (threadIdx.x == 0) {
     if (!(sv[0] > 0.0) || si[0] != p) atomicExch(err, 3);
     piv[(size_t)m * n + k] = p;
     um[p] = 1;
     const double2 pk = Am[p + (size_t)n * k];
-    dinv[m] = (pk.x == 0.0 && pk.y == 0.0) ? make_double2(0.0, 0.0) : crecip(pk);
+    sd = (pk.x == 0.0 && pk.y == 0.0) ? make_double2(0.0, 0.0) : crecip(pk);
+    dinv[m] = sd;
   }
+  __syncthreads();
+  const double2 d = sd;
+  // prow: the pivot row; fcol: the pivot column times the pivot's reciprocal
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     prow[(size_t)m * n + j] = Am[p + (size_t)n * j];
-    fcol[(size_t)m * n + j] = Am[j + (size_t)n * k];
+    fcol[(size_t)m * n + j] = cmul(Am[j + (size_t)n * k], d);
   }
 }
 
@@ -129,9 +135,15 @@ __global__ void __launch_bounds__(256) gj_update_kernel(double2 *__restrict__ A,
   if (i == p) {
     *a = (j == k) ? d : cmul(pj, d);
   } else {
-    const double2 f = cmul(fcol[(size_t)m * n + i], d);
-    if (j == k) *a = make_double2(-f.x, -f.y);
-    else *a = csub(*a, cmul(f, pj));
+    const double2 f = fcol[(size_t)m * n + i];
+    if (j == k) {
+      *a = make_double2(-f.x, -f.y);
+    } else {
+      double2 v = *a;  // a - f pj in four FMAs
+      v.x = fma(-f.x, pj.x, v.x); v.x = fma(f.y, pj.y, v.x);
+      v.y = fma(-f.x, pj.y, v.y); v.y = fma(-f.y, pj.x, v.y);
+      *a = v;
+    }
   }
 }
 
