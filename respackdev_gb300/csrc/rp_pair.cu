@@ -154,7 +154,8 @@ constexpr int PD_THREADS = 160;
 constexpr int PD_CGMAX = 16;  // pass-1 output frequencies per register group, at most
 
 // pass-1 register group for D2 output frequencies: an even count (the twiddles
-// are read in 16-byte pairs) from a few compiled widths
+// are read in 16-byte pairs) from a few compiled widths; above 14 frequencies
+// the groups are 16 wide, so every group starts at a multiple of 4
 __host__ __device__ inline int pd_group(int D2) {
   const int need = (D2 + 1) & ~1;
   return need <= 8 ? 8 : need <= 12 ? 12 : need <= 14 ? 14 : 16;
@@ -168,7 +169,9 @@ struct PdLayout {
 __host__ __device__ inline size_t pd_up16(size_t b) { return (b + 15) & ~(size_t)15; }
 
 // Shared-memory carve-up of pair_slab_kernel (host and device agree on it).
-//   TW2 [n2][D2P] float2, zero beyond D2      TW1 [n1][D1P] float2, zero beyond D1
+//   TW2 [n2][D2P] float2, zero beyond D2 (direct y pass), or, split y pass:
+//       [n2/4][D2P] twiddles e^{+2 pi i c b / n2} then the n2 phases e^{-2 pi i f0 y / n2}
+//   TW1 [n1][D1P] float2, zero beyond D1
 //   TZ  [2][n3]  float2 (z twiddles of the slab, double-buffered by slab parity)
 //   X   [nq][SQ] float4: row x at x*D2X, column c2 -> (pair 2q, pair 2q+1)
 //   Y   [jmax][D2][D1] float2        acc [jmax][ng] float2
@@ -212,7 +215,14 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.x, b.y, -a.y * b.x));
 }
 
-template <int CG>
+// The y pass, direct (SPLIT false) or split (SPLIT true: n2 = 4 s, the sphere
+// inside the box).  The split form writes y = s a + b; the output frequencies
+// of the register group are f0 - c (c = 0 .. D2-1), so
+//   X[c] = sum_b e^{+2 pi i c b / n2} Q_b[c mod 4],
+//   Q_b[r] = sum_a i^{r a} P[s a + b] e^{-2 pi i f0 (s a + b) / n2},
+// a radix-4 butterfly of additions per b instead of four twiddle products per
+// frequency: about 2.6 times fewer FP32 instructions than the direct sum.
+template <int CG, bool SPLIT>
 __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *__restrict__ ur, PairArgs a,
                                                                    float2 *__restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -234,9 +244,19 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
   for (int j = tid; j < D1; j += PD_THREADS) f1[j] = c1 ? modp2(-(j - a.R1) - s1, n1) : j;
   for (int j = tid; j < D2; j += PD_THREADS) f2[j] = c2 ? modp2(-(j - a.R2) - s2, n2) : j;
   __syncthreads();
-  for (int i = tid; i < n2 * L.D2P; i += PD_THREADS) {
-    const int y = i / L.D2P, c = i % L.D2P;
-    TW2[i] = c < D2 ? tw32((f2[c] * y) % n2, n2) : make_float2(0.f, 0.f);
+  const int rows4 = n2 / 4;  // split y pass: rows per residue class
+  float2 *PH = TW2 + (size_t)rows4 * L.D2P;
+  if (SPLIT) {
+    for (int i = tid; i < rows4 * L.D2P; i += PD_THREADS) {
+      const int b = i / L.D2P, c = i % L.D2P;
+      TW2[i] = c < D2 ? tw32((n2 - (c * b) % n2) % n2, n2) : make_float2(0.f, 0.f);
+    }
+    for (int y = tid; y < n2; y += PD_THREADS) PH[y] = tw32((f2[0] * y) % n2, n2);
+  } else {
+    for (int i = tid; i < n2 * L.D2P; i += PD_THREADS) {
+      const int y = i / L.D2P, c = i % L.D2P;
+      TW2[i] = c < D2 ? tw32((f2[c] * y) % n2, n2) : make_float2(0.f, 0.f);
+    }
   }
   for (int i = tid; i < n1 * L.D1P; i += PD_THREADS) {
     const int x = i / L.D1P, c = i % L.D1P;
@@ -279,8 +299,50 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
         float2 sa[CG], sb[CG];
 #pragma unroll
         for (int c = 0; c < CG; c++) { sa[c] = make_float2(0.f, 0.f); sb[c] = sa[c]; }
-        const float4 *twr = (const float4 *)(TW2 + cg);
-        auto step = [&](float2 v, float2 va, float2 vb, int y) {
+        if (SPLIT) {
+          // four rows (s a + b, a = 0..3) per step; the next step's rows in flight
+          float2 nv[4], na[4], nb[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            const size_t o = zo + (size_t)(u * rows4) * n1;
+            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
+          }
+          for (int b = 0; b < rows4; b++) {
+            float2 PA[4], PB[4];
+            const int bn = min(b + 1, rows4 - 1);
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const float2 v = cmulc(nv[u], PH[u * rows4 + b]), va = na[u], vb = nb[u];
+              const size_t o = zo + (size_t)(u * rows4 + bn) * n1;
+              nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
+              PA[u] = cmul(v, va); PB[u] = cmul(v, vb);
+            }
+            // Q[r] = sum_a i^{r a} P[a]
+            float2 QA[4], QB[4];
+            auto bfly = [](const float2 *P, float2 *Q) {
+              const float2 t0 = make_float2(P[0].x + P[2].x, P[0].y + P[2].y);
+              const float2 t1 = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
+              const float2 t2 = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
+              const float2 t3 = make_float2(P[1].x - P[3].x, P[1].y - P[3].y);
+              Q[0] = make_float2(t0.x + t2.x, t0.y + t2.y);
+              Q[2] = make_float2(t0.x - t2.x, t0.y - t2.y);
+              Q[1] = make_float2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+              Q[3] = make_float2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+            };
+            bfly(PA, QA);
+            bfly(PB, QB);
+            const float4 *t = (const float4 *)(TW2 + (size_t)b * L.D2P + cg);
+#pragma unroll
+            for (int c = 0; c < CG / 2; c++) {
+              const float4 w = t[c];
+              const float2 w0 = make_float2(w.x, w.y), w1 = make_float2(w.z, w.w);
+              cfma(sa[2 * c], QA[(2 * c) & 3], w0); cfma(sb[2 * c], QB[(2 * c) & 3], w0);
+              cfma(sa[2 * c + 1], QA[(2 * c + 1) & 3], w1); cfma(sb[2 * c + 1], QB[(2 * c + 1) & 3], w1);
+            }
+          }
+        } else {
+          const float4 *twr = (const float4 *)(TW2 + cg);
+          auto step = [&](float2 v, float2 va, float2 vb, int y) {
           const float2 PA = cmulc(v, va), PB = cmulc(v, vb);
           const float4 *t = twr + (size_t)y * (L.D2P / 2);
 #pragma unroll
@@ -313,6 +375,7 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
 #pragma unroll
         for (int u = 0; u < 3; u++)
           if (n2f + u < n2) step(nv[u], na[u], nb[u], n2f + u);
+        }
         float4 *xr = X + (size_t)q1 * L.SQ + (size_t)x1 * L.D2X + cg;
 #pragma unroll
         for (int c = 0; c < CG; c++)
@@ -407,12 +470,15 @@ int launch_pair_density_fp32(const float2 *ur, const PairGeom &g, const PairChun
   if (g.ntk > 65535) fail(1, "more than 65535 k points in one pair-density launch");
   const size_t smem = pair_density_smem(g, c.jmax, false);
   if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
-  const int D2 = 2 * g.R2 + 1 <= g.n2 ? 2 * g.R2 + 1 : g.n2;
-  auto kern = pair_slab_kernel<16>;
+  const bool inside = 2 * g.R2 + 1 <= g.n2;
+  const int D2 = inside ? 2 * g.R2 + 1 : g.n2;
+  // split y pass when the box length divides by 4 and the sphere fits in the box
+  const bool split = inside && g.n2 % 4 == 0;
+  auto kern = split ? pair_slab_kernel<16, true> : pair_slab_kernel<16, false>;
   switch (pd_group(D2)) {
-    case 8: kern = pair_slab_kernel<8>; break;
-    case 12: kern = pair_slab_kernel<12>; break;
-    case 14: kern = pair_slab_kernel<14>; break;
+    case 8: kern = split ? pair_slab_kernel<8, true> : pair_slab_kernel<8, false>; break;
+    case 12: kern = split ? pair_slab_kernel<12, true> : pair_slab_kernel<12, false>; break;
+    case 14: kern = split ? pair_slab_kernel<14, true> : pair_slab_kernel<14, false>; break;
     default: break;
   }
   RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
