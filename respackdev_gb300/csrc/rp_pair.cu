@@ -150,6 +150,8 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
 //                one G of the sphere (about 30 of the 52 tiles of a 13x13
 //                square); both pairs of the couple per load.
 //   z term:      acc[j][g] += Y[j][c2(g)][c1(g)] e^{-2 pi i f3(g) z / n3}.
+// Y and acc hold the two pairs of a couple side by side (float4), so the z
+// term moves both with one 16-byte access.
 constexpr int PD_THREADS = 160;
 constexpr int PD_CGMAX = 16;  // pass-1 output frequencies per register group, at most
 
@@ -171,10 +173,10 @@ __host__ __device__ inline size_t pd_up16(size_t b) { return (b + 15) & ~(size_t
 // Shared-memory carve-up of pair_slab_kernel (host and device agree on it).
 //   TW2 [n2][D2P] float2, zero beyond D2 (direct y pass), or, split y pass:
 //       [n2/4][D2P] twiddles e^{+2 pi i c b / n2} then the n2 phases e^{-2 pi i f0 y / n2}
-//   TW1 [n1][D1P] float2, zero beyond D1
+//   TW1 [n1][D1P] float2, zero beyond D1, or, split x pass: [n1/4][D1P] then n1 phases
 //   TZ  [2][n3]  float2 (z twiddles of the slab, double-buffered by slab parity)
 //   X   [nq][SQ] float4: row x at x*D2X, column c2 -> (pair 2q, pair 2q+1)
-//   Y   [jmax][D2][D1] float2        acc [jmax][ng] float2
+//   Y   [nq][D2][D1] float4          acc [nq][ng] float4 (pair 2q, pair 2q+1)
 //   sel [ng] int: c1 | c2 << 10 | f3 << 20          f1 [D1], f2 [D2] int
 //   tile flags [ntl] and tile list [ntl + 1] int, ntl = (D1P / 4) D2, tile = grp D2 + c2
 // D2X is odd and SQ = D2X (mod 8), so the 16-byte column stores of pass 1 and
@@ -195,8 +197,8 @@ __host__ __device__ inline PdLayout pd_layout(int n1, int n2, int n3, int R1, in
   L.oTW1 = o; o += pd_up16(sizeof(float2) * (size_t)n1 * L.D1P);
   L.oTZ = o;  o += pd_up16(sizeof(float2) * 2 * (size_t)n3);
   L.oX = o;   o += sizeof(float4) * (size_t)L.nq * L.SQ;
-  L.oY = o;   o += pd_up16(sizeof(float2) * (size_t)jmax * L.D1 * L.D2);
-  L.oAcc = o; o += pd_up16(sizeof(float2) * (size_t)jmax * ng);
+  L.oY = o;   o += sizeof(float4) * (size_t)L.nq * L.D1 * L.D2;
+  L.oAcc = o; o += sizeof(float4) * (size_t)L.nq * ng;
   L.oSel = o; o += pd_up16(sizeof(int) * (size_t)ng);
   L.oF = o;   o += pd_up16(sizeof(int) * (size_t)(L.D1 + L.D2));
   L.ntl = (L.D1P / 4) * L.D2;
@@ -210,18 +212,32 @@ __device__ __forceinline__ float2 tw32(int j, int n) {
   sincospif(-2.0f * j / n, &s, &c);
   return make_float2(c, s);
 }
+// Q[r] = sum_a i^{r a} P[a], a, r = 0..3
+__device__ __forceinline__ void bfly4(const float2 *P, float2 *Q) {
+  const float2 t0 = make_float2(P[0].x + P[2].x, P[0].y + P[2].y);
+  const float2 t1 = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
+  const float2 t2 = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
+  const float2 t3 = make_float2(P[1].x - P[3].x, P[1].y - P[3].y);
+  Q[0] = make_float2(t0.x + t2.x, t0.y + t2.y);
+  Q[2] = make_float2(t0.x - t2.x, t0.y - t2.y);
+  Q[1] = make_float2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
+  Q[3] = make_float2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
+}
 // conj(a) * b
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.x, b.y, -a.y * b.x));
 }
 
-// The y pass, direct (SPLIT false) or split (SPLIT true: n2 = 4 s, the sphere
-// inside the box).  The split form writes y = s a + b; the output frequencies
-// of the register group are f0 - c (c = 0 .. D2-1), so
+// The y and x passes, direct (SPLIT false) or split (SPLIT true: n1 and n2
+// multiples of 4, the sphere inside the box).  The split form writes
+// y = s a + b (s = n2/4); the output frequencies of the register group are
+// f0 - c (c = 0 .. D2-1), so
 //   X[c] = sum_b e^{+2 pi i c b / n2} Q_b[c mod 4],
 //   Q_b[r] = sum_a i^{r a} P[s a + b] e^{-2 pi i f0 (s a + b) / n2},
 // a radix-4 butterfly of additions per b instead of four twiddle products per
-// frequency: about 2.6 times fewer FP32 instructions than the direct sum.
+// frequency: about 2.6 times fewer FP32 instructions than the direct sum.  The
+// x pass is split the same way; its phase e^{-2 pi i f1_0 x / n1} is applied
+// when pass 1 stores X.
 template <int CG, bool SPLIT>
 __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *__restrict__ ur, PairArgs a,
                                                                    float2 *__restrict__ out) {
@@ -237,7 +253,7 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
   const int nq = (cnt + 1) / 2;
   float2 *TW2 = (float2 *)smem, *TW1 = (float2 *)(smem + L.oTW1), *TZ = (float2 *)(smem + L.oTZ);
   float4 *X = (float4 *)(smem + L.oX);
-  float2 *Y = (float2 *)(smem + L.oY), *acc = (float2 *)(smem + L.oAcc);
+  float4 *Y = (float4 *)(smem + L.oY), *acc = (float4 *)(smem + L.oAcc);
   int *gsel = (int *)(smem + L.oSel), *f1 = (int *)(smem + L.oF), *f2 = f1 + D1;
   int *tflag = (int *)(smem + L.oTile), *tlist = tflag + L.ntl;  // tlist[0] = count
   for (int i = tid; i < L.ntl; i += PD_THREADS) tflag[i] = 0;
@@ -258,9 +274,19 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
       TW2[i] = c < D2 ? tw32((f2[c] * y) % n2, n2) : make_float2(0.f, 0.f);
     }
   }
-  for (int i = tid; i < n1 * L.D1P; i += PD_THREADS) {
-    const int x = i / L.D1P, c = i % L.D1P;
-    TW1[i] = c < D1 ? tw32((f1[c] * x) % n1, n1) : make_float2(0.f, 0.f);
+  const int cols4 = n1 / 4;  // split x pass: columns per residue class
+  float2 *PH1 = TW1 + (size_t)cols4 * L.D1P;
+  if (SPLIT) {
+    for (int i = tid; i < cols4 * L.D1P; i += PD_THREADS) {
+      const int b = i / L.D1P, c = i % L.D1P;
+      TW1[i] = c < D1 ? tw32((n1 - (c * b) % n1) % n1, n1) : make_float2(0.f, 0.f);
+    }
+    for (int x = tid; x < n1; x += PD_THREADS) PH1[x] = tw32((f1[0] * x) % n1, n1);
+  } else {
+    for (int i = tid; i < n1 * L.D1P; i += PD_THREADS) {
+      const int x = i / L.D1P, c = i % L.D1P;
+      TW1[i] = c < D1 ? tw32((f1[c] * x) % n1, n1) : make_float2(0.f, 0.f);
+    }
   }
   for (int g = tid; g < ng; g += PD_THREADS) {
     const int *l = a.lg0 + 3 * g;
@@ -270,7 +296,7 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
     gsel[g] = i1 | (i2 << 10) | (i3 << 20);
     tflag[(i1 >> 2) * D2 + i2] = 1;
   }
-  for (int i = tid; i < cnt * ng; i += PD_THREADS) acc[i] = make_float2(0.f, 0.f);
+  for (int i = tid; i < nq * ng; i += PD_THREADS) acc[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   __syncthreads();
   if (tid < 32) {  // compact the flagged tiles in (group, c2) order; read after pass 1's barrier
     int n = 0;
@@ -317,20 +343,9 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
               nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
               PA[u] = cmul(v, va); PB[u] = cmul(v, vb);
             }
-            // Q[r] = sum_a i^{r a} P[a]
             float2 QA[4], QB[4];
-            auto bfly = [](const float2 *P, float2 *Q) {
-              const float2 t0 = make_float2(P[0].x + P[2].x, P[0].y + P[2].y);
-              const float2 t1 = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
-              const float2 t2 = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
-              const float2 t3 = make_float2(P[1].x - P[3].x, P[1].y - P[3].y);
-              Q[0] = make_float2(t0.x + t2.x, t0.y + t2.y);
-              Q[2] = make_float2(t0.x - t2.x, t0.y - t2.y);
-              Q[1] = make_float2(t1.x - t3.y, t1.y + t3.x);  // t1 + i t3
-              Q[3] = make_float2(t1.x + t3.y, t1.y - t3.x);  // t1 - i t3
-            };
-            bfly(PA, QA);
-            bfly(PB, QB);
+            bfly4(PA, QA);
+            bfly4(PB, QB);
             const float4 *t = (const float4 *)(TW2 + (size_t)b * L.D2P + cg);
 #pragma unroll
             for (int c = 0; c < CG / 2; c++) {
@@ -377,9 +392,13 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
           if (n2f + u < n2) step(nv[u], na[u], nb[u], n2f + u);
         }
         float4 *xr = X + (size_t)q1 * L.SQ + (size_t)x1 * L.D2X + cg;
+        const float2 ph1 = SPLIT ? PH1[x1] : make_float2(1.f, 0.f);
 #pragma unroll
         for (int c = 0; c < CG; c++)
-          if (cg + c < D2) xr[c] = make_float4(sa[c].x, sa[c].y, sb[c].x, sb[c].y);
+          if (cg + c < D2) {
+            const float2 va = SPLIT ? cmul(sa[c], ph1) : sa[c], vb = SPLIT ? cmul(sb[c], ph1) : sb[c];
+            xr[c] = make_float4(va.x, va.y, vb.x, vb.y);
+          }
       }
     }
     __syncthreads();
@@ -391,25 +410,42 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
 #pragma unroll
       for (int c = 0; c < 4; c++) { ya[c] = make_float2(0.f, 0.f); yb[c] = ya[c]; }
       const float4 *xc = X + (size_t)q * L.SQ + cc2;
-      const float4 *tw = (const float4 *)(TW1 + 4 * grp);
-#pragma unroll 4
-      for (int x = 0; x < n1; x++) {
-        const float4 v = xc[(size_t)x * L.D2X];
-        const float2 va = make_float2(v.x, v.y), vb = make_float2(v.z, v.w);
-        const float4 t0 = tw[(size_t)x * (L.D1P / 2)], t1 = tw[(size_t)x * (L.D1P / 2) + 1];
-        const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
-                             make_float2(t1.z, t1.w)};
+      if (SPLIT) {
+        // x = s a + b; residue r of c1 = 4 grp + r is r
+        for (int b = 0; b < cols4; b++) {
+          float2 PA[4], PB[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) { cfma(ya[c], va, w[c]); cfma(yb[c], vb, w[c]); }
+          for (int u = 0; u < 4; u++) {
+            const float4 v = xc[(size_t)(u * cols4 + b) * L.D2X];
+            PA[u] = make_float2(v.x, v.y); PB[u] = make_float2(v.z, v.w);
+          }
+          float2 QA[4], QB[4];
+          bfly4(PA, QA);
+          bfly4(PB, QB);
+          const float4 *tw = (const float4 *)(TW1 + (size_t)b * L.D1P + 4 * grp);
+          const float4 t0 = tw[0], t1 = tw[1];
+          const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
+                               make_float2(t1.z, t1.w)};
+#pragma unroll
+          for (int c = 0; c < 4; c++) { cfma(ya[c], QA[c], w[c]); cfma(yb[c], QB[c], w[c]); }
+        }
+      } else {
+        const float4 *tw = (const float4 *)(TW1 + 4 * grp);
+#pragma unroll 4
+        for (int x = 0; x < n1; x++) {
+          const float4 v = xc[(size_t)x * L.D2X];
+          const float2 va = make_float2(v.x, v.y), vb = make_float2(v.z, v.w);
+          const float4 t0 = tw[(size_t)x * (L.D1P / 2)], t1 = tw[(size_t)x * (L.D1P / 2) + 1];
+          const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
+                               make_float2(t1.z, t1.w)};
+#pragma unroll
+          for (int c = 0; c < 4; c++) { cfma(ya[c], va, w[c]); cfma(yb[c], vb, w[c]); }
+        }
       }
-      float2 *yA = Y + (size_t)(2 * q) * D1 * D2 + (size_t)cc2 * D1 + 4 * grp;
-      const bool hasB = 2 * q + 1 < cnt;
+      float4 *yq = Y + (size_t)q * D1 * D2 + (size_t)cc2 * D1 + 4 * grp;
 #pragma unroll
       for (int c = 0; c < 4; c++)
-        if (4 * grp + c < D1) {
-          yA[c] = ya[c];
-          if (hasB) yA[(size_t)D1 * D2 + c] = yb[c];
-        }
+        if (4 * grp + c < D1) yq[c] = make_float4(ya[c].x, ya[c].y, yb[c].x, yb[c].y);
     }
     __syncthreads();
     // z term (overlaps the next slab's pass 1, which touches neither Y nor this tz)
@@ -417,7 +453,14 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
       const int sel = gsel[g];
       const int yi = (sel & 1023) + D1 * ((sel >> 10) & 1023);
       const float2 t = tz[sel >> 20];
-      for (int j = 0; j < cnt; j++) cfma(acc[(size_t)j * ng + g], Y[(size_t)j * D1 * D2 + yi], t);
+      for (int q = 0; q < nq; q++) {
+        const float4 yv = Y[(size_t)q * D1 * D2 + yi];
+        float4 &av = acc[(size_t)q * ng + g];
+        float2 sA = make_float2(av.x, av.y), sB = make_float2(av.z, av.w);
+        cfma(sA, make_float2(yv.x, yv.y), t);
+        cfma(sB, make_float2(yv.z, yv.w), t);
+        av = make_float4(sA.x, sA.y, sB.x, sB.y);
+      }
     }
   }
   __syncthreads();
@@ -425,8 +468,10 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
   for (int jj = 0; jj < cnt; jj++) {
     const int p = a.pair_list[first + jj];
     float2 *dst = out + ((size_t)p * a.ntk + k) * ng;
+    const float4 *src = acc + (size_t)(jj >> 1) * ng;
     for (int g = tid; g < ng; g += PD_THREADS) {
-      const float2 v = acc[(size_t)jj * ng + g];
+      const float4 v4 = src[g];
+      const float2 v = (jj & 1) ? make_float2(v4.z, v4.w) : make_float2(v4.x, v4.y);
       dst[g] = make_float2(v.x * inv, v.y * inv);
     }
   }
@@ -472,8 +517,8 @@ int launch_pair_density_fp32(const float2 *ur, const PairGeom &g, const PairChun
   if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
   const bool inside = 2 * g.R2 + 1 <= g.n2;
   const int D2 = inside ? 2 * g.R2 + 1 : g.n2;
-  // split y pass when the box length divides by 4 and the sphere fits in the box
-  const bool split = inside && g.n2 % 4 == 0;
+  // split y and x passes when both box lengths divide by 4 and the sphere fits in the box
+  const bool split = inside && 2 * g.R1 + 1 <= g.n1 && g.n2 % 4 == 0 && g.n1 % 4 == 0;
   auto kern = split ? pair_slab_kernel<16, true> : pair_slab_kernel<16, false>;
   switch (pd_group(D2)) {
     case 8: kern = split ? pair_slab_kernel<8, true> : pair_slab_kernel<8, false>; break;
