@@ -212,6 +212,10 @@ __device__ __forceinline__ float2 tw32(int j, int n) {
   sincospif(-2.0f * j / n, &s, &c);
   return make_float2(c, s);
 }
+// L2 prefetch of a contiguous range (16-byte aligned, a multiple of 16 bytes)
+__device__ __forceinline__ void l2_prefetch_bulk(const void *p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 // Q[r] = sum_a i^{r a} P[a], a, r = 0..3
 __device__ __forceinline__ void bfly4(const float2 *P, float2 *Q) {
   const float2 t0 = make_float2(P[0].x + P[2].x, P[0].y + P[2].y);
@@ -310,9 +314,15 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
   }
   const size_t bstride = (size_t)n12 * n3;
   const float2 *uvir = ur + ((size_t)kq * a.ncb + vir) * bstride, *uocc = ur + (size_t)k * a.ncb * bstride;
+  // the virtual band is read by this CTA alone, straight from HBM: its slab two
+  // ahead is pulled into L2 by one bulk prefetch per slab (16-byte multiples)
+  const bool pf = (n12 % 2) == 0;
+  if (pf && tid == 0)
+    for (int z = 0; z < min(2, n3); z++) l2_prefetch_bulk(uvir + (size_t)z * n12, (unsigned)(n12 * sizeof(float2)));
   for (int z = 0; z < n3; z++) {
     float2 *tz = TZ + (z & 1) * n3;
     for (int i = tid; i < n3; i += PD_THREADS) tz[i] = tw32((i * z) % n3, n3);
+    if (pf && tid == 0 && z + 2 < n3) l2_prefetch_bulk(uvir + (size_t)(z + 2) * n12, (unsigned)(n12 * sizeof(float2)));
     // pass 1: row = (couple q1, column x1); one row per thread when nq n1 <= PD_THREADS
     for (int row = tid; row < nq * n1; row += PD_THREADS) {
       const int q1 = row / n1, x1 = row - q1 * n1;
