@@ -40,7 +40,8 @@ __device__ __forceinline__ cx operator/(cx a, cx b) {
 __device__ __forceinline__ cx operator/(cx a, double s) { return cx(a.r / s, a.i / s); }
 __device__ __forceinline__ cx operator/(double s, cx b) { return cx(s, 0) / b; }
 __device__ __forceinline__ double cabs_(cx a) { return hypot(a.r, a.i); }
-__device__ __forceinline__ cx clog_(cx a) { return cx(log(hypot(a.r, a.i)), atan2(a.i, a.r)); }
+// log z = log|z| + i arg z, with log|z| = log(|z|^2) / 2 (|z| of order one here)
+__device__ __forceinline__ cx clog_(cx a) { return cx(0.5 * log(fma(a.r, a.r, a.i * a.i)), atan2(a.i, a.r)); }
 
 // ---- closed forms (m_tetrahedron_20170325.F:304-451), one frequency w ----
 __device__ cx s1g30g21(cx g0, cx g1, cx w) {
@@ -447,6 +448,116 @@ __device__ __forceinline__ bool degen_terms(const Chk &c, const Pt (&v)[4], cons
   }
 }
 
+// Tetrahedron categories: the normal closed forms, the near-degenerate forms of
+// chk1's cases 2, 3, 4 (i3 = 2) and 4 (i3 = 3..6) on an uncut tetrahedron, and
+// the rest (cut by the Fermi level, or a case calc() does not know).
+enum { TC_NORMAL = 0, TC_S2, TC_S3, TC_S4A, TC_S4B, TC_OTHER, TC_NCAT, TC_SKIP = 255 };
+
+// One uncut near-degenerate (tetrahedron, sign) of category cat.  The forms are
+// those of degen_terms with every real difference of the tetrahedron turned
+// into a product of a few reciprocals once, outside the frequency loop: per
+// frequency only complex products and the averaged points' logs remain.
+__device__ void degen_tetra(const TetraArgs &a, int code, int cat, const double *e1m, const double *e2m,
+                            const double2 *Lt, int e0, int ne, int nec, double2 *xo) {
+  const int t = code >> 1, sg = code & 1;
+  const double dsgn = sg == 0 ? 1.0 : -1.0, dg = a.delt * dsgn;
+  int slot[4];
+  double g[4];
+  cx ffk[4], ggk[4];
+  for (int v = 0; v < 4; v++) {
+    slot[v] = a.imt1[4 * t + v];
+    ggk[v] = cx(-(e2m[slot[v]] - e1m[slot[v]]), a.delt) * dsgn;
+    ffk[v] = cx(dsgn, 0);
+    g[v] = ggk[v].r;
+  }
+  const Chk c = chk1(a.dmna, a.dmnr, ggk);
+  // the permuted vertices as scalars: slots (output rows), energies and log rows
+  const int i0 = c.ia3[0], i1 = c.ia3[1], i2 = c.ia3[2], i3 = c.ia3[3], j0 = c.ia4[0], j1 = c.ia4[1];
+  const int sa0 = slot[i0], sa1 = slot[i1], sa2 = slot[i2], sa3 = slot[i3], sb0 = slot[j0], sb1 = slot[j1];
+  const double ga0 = g[i0], ga1 = g[i1], ga2 = g[i2], ga3 = g[i3], gb0 = g[j0], gb1 = g[j1];
+  const double2 *Lb0 = Lt + ((size_t)sg * a.ntk + sb0) * nec, *Lb1 = Lt + ((size_t)sg * a.ntk + sb1) * nec;
+  auto put = [&](int sl, int e, cx v) { sadd(&xo[sl * nec + e], v); };
+  // z on the real axis: the reference's ratio logs through calc()
+  auto on_axis = [&](cx w, int e) {
+    cx x[4];
+    if (!calc_w(c, ffk, ggk, w, x)) { atomicExch(a.err, 2); return; }
+    for (int v = 0; v < 4; v++) put(slot[v], e, x[v]);
+  };
+  if (cat == TC_S2) {
+    const double qg = (ga0 + ga1) / 2.0;
+    const double d2 = qg - gb0, d3 = qg - gb1, d23 = gb0 - gb1;
+    const double r2 = 1.0 / d2, r3 = 1.0 / d3, r23 = 1.0 / d23;
+    const double r22 = r2 * r2, r33 = r3 * r3;
+    // sub2g10 (c1), sub2g30 (c2), sub1g30 (c3) of calc's case 2
+    const double K1 = r22 * r33 / 12.0, K2 = r22 * r2 * r23 / 6.0, K3 = r33 * r3 * r23 / 6.0;
+    const double K4 = r3 * r22 * r23 / 6.0, K5 = r33 * r22 * r2 / 6.0, K6 = r22 * r2 * r23 * r23 / 6.0;
+    const double K7 = 0.5 * r2, K8 = 0.5 * r22 * r33, K9 = -0.5 * r22 * r23, K10 = 0.5 * r2 * r3;
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      if (dg + w.i == 0.0) { on_axis(w, e); continue; }
+      const cx Zq(qg + w.r, dg + w.i), Z0(gb0 + w.r, dg + w.i), Z1(gb1 + w.r, dg + w.i);
+      const cx Lq = clog_(Zq), L0(Lb0[e].x, Lb0[e].y), L1(Lb1[e].x, Lb1[e].y);
+      const cx Zq2 = Zq * Zq, Z02 = Z0 * Z0, Z12 = Z1 * Z1, Z01 = Z0 * Z1;
+      const cx c1 = Zq * (Zq2 + 5.0 * Z01 - 3.0 * Zq * (Z0 + Z1)) * K1 - Z02 * Z0 * (L0 - Lq) * K2 +
+                    Z12 * Z1 * (L1 - Lq) * K3;
+      const cx c2 = (Zq2 * d23 + Z02 * d3) * K4 - Zq2 * (2.0 * Z0 * d3 + Z1 * d2) * (Lq - L1) * K5 +
+                    Z02 * (2.0 * Zq * d23 - Z1 * d2) * (L0 - L1) * K6;
+      const cx c3 = cx(K7, 0.0) - Zq * (-2.0 * Z01 + Zq * (Z1 + Z0)) * (Lq - L1) * K8 + Z02 * (L1 - L0) * K9 +
+                    Z1 * K10;
+      put(sa0, e, c1 * dsgn);
+      put(sa1, e, c1 * dsgn);
+      put(sb0, e, c2 * dsgn);
+      put(sb1, e, (c3 - c2 - c1 - c1) * dsgn);
+    }
+  } else if (cat == TC_S3) {
+    const double qg = (ga0 + ga1 + ga2) / 3.0;
+    const double r = 1.0 / (qg - gb0), r2 = r * r, r3 = r2 * r;
+    // sub2g30g10 (c1), sub1g30g20 (c2)
+    const double K1 = r3 / 36.0, K2 = r3 * r / 6.0, K3 = 0.25 * r2, K4 = 0.5 * r3;
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      if (dg + w.i == 0.0) { on_axis(w, e); continue; }
+      const cx Zq(qg + w.r, dg + w.i), Zp(gb0 + w.r, dg + w.i);
+      const cx dL = clog_(Zq) - cx(Lb0[e].x, Lb0[e].y), Zp2 = Zp * Zp;
+      const cx c1 = (2.0 * Zq * Zq - 7.0 * Zq * Zp + 11.0 * Zp2) * K1 - Zp2 * Zp * dL * K2;
+      const cx c2 = (Zq - 3.0 * Zp) * K3 + Zp2 * dL * K4;
+      put(sa0, e, c1 * dsgn);
+      put(sa1, e, c1 * dsgn);
+      put(sa2, e, c1 * dsgn);
+      put(sb0, e, (c2 - c1 - c1 - c1) * dsgn);
+    }
+  } else if (cat == TC_S4A) {
+    const double q1g = (ga0 + ga1) / 2.0, q2g = (ga2 + ga3) / 2.0;
+    const double d = q1g - q2g, r = 1.0 / d, r2 = r * r, r3 = r2 * r;
+    // sub2g30g20 (c1), sub1g30g21 (c2)
+    const double K1 = r3 / 12.0, K2 = 0.5 * r3 * r, K3 = 0.5 * r2;
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      if (dg + w.i == 0.0) { on_axis(w, e); continue; }
+      const cx Z1(q1g + w.r, dg + w.i), Z2(q2g + w.r, dg + w.i);
+      const cx dL = clog_(Z1) - clog_(Z2), Z12 = Z1 * Z2;
+      const cx c1 = (d * (Z1 + 2.0 * Z2) - 6.0 * Z12) * K1 + Z12 * Z2 * dL * K2;
+      const cx c2 = (Z1 + Z2) * K3 - dL * Z12 * r3;
+      const cx h = (c2 - c1 - c1) * 0.5 * dsgn;
+      put(sa0, e, c1 * dsgn);
+      put(sa1, e, c1 * dsgn);
+      put(sa2, e, h);
+      put(sa3, e, h);
+    }
+  } else {  // TC_S4B: sub2simple at the average of all four
+    const double s4 = (ga0 + ga1 + ga2 + ga3) / 4.0;
+    for (int e = 0; e < ne; e++) {
+      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
+      if (dg + w.i == 0.0) { on_axis(w, e); continue; }
+      const cx c1 = 1.0 / (cx(s4 + w.r, dg + w.i) * 24.0) * dsgn;
+      put(sa0, e, c1);
+      put(sa1, e, c1);
+      put(sa2, e, c1);
+      put(sa3, e, c1);
+    }
+  }
+}
+
 // One (tetrahedron, sign) that is near-degenerate or cut by the Fermi level:
 // ttct and the reference's closed forms (m_tetrahedron_20170325.F:99-302).
 // Out of line, so that its large local arrays do not weigh on the normal path.
@@ -524,10 +635,11 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
   double2 *xo = (double2 *)smem;               // ntk * nec
   double2 *Lt = xo + (size_t)ntk * nec;        // [sign][mesh slot][e] log(g + w)
   double *e1m = (double *)(Lt + 2 * (size_t)ntk * nec), *e2m = e1m + ntk;
-  int *lists = (int *)(e2m + ntk);             // 2*ntet entries: normal from the front, others from the back
-  __shared__ int n_normal, n_other;
+  int *lists = (int *)(e2m + ntk);             // 2*ntet entries, one segment per category
+  unsigned char *tcat = (unsigned char *)(lists + 2 * (size_t)ntet);  // category of each tetrahedron
+  __shared__ int ncat[TC_NCAT], cbeg[TC_NCAT + 1], cur[TC_NCAT];
   const int bv = a.pair_vir[p], bo = a.pair_occ[p];
-  if (threadIdx.x == 0) { n_normal = 0; n_other = 0; }
+  if (threadIdx.x < TC_NCAT) ncat[threadIdx.x] = 0;
   for (int i = threadIdx.x; i < ntk * nec; i += blockDim.x) xo[i] = make_double2(0, 0);
   for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
     int k = a.index_kpt[m];
@@ -545,8 +657,7 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
     const cx L = clog_(z);
     Lt[((size_t)sg * ntk + m) * nec + e] = make_double2(L.r, L.i);
   }
-  // classify: normal tetrahedra (both signs) from the front as t, the others
-  // from the back as 2*t + sign.  chk1 sees |g_a - g_b| and |g_a + g_b|, which
+  // classify every tetrahedron.  chk1 sees |g_a - g_b| and |g_a + g_b|, which
   // the sign does not change, so one test covers both signs.
   for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
     double ee1[4], ee2[4];
@@ -554,22 +665,42 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
     const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
     const double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
     const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
-    if (mx2 <= f) continue;  // ttct(+1) drops the whole tetrahedron
-    bool normal = false;
-    if (mn2 > f && mx1 < f) {
+    int cat = TC_OTHER;
+    if (mx2 <= f) {
+      cat = TC_SKIP;  // ttct(+1) drops the whole tetrahedron
+    } else if (mn2 > f && mx1 < f) {
       cx ggk[4];
       for (int v = 0; v < 4; v++) ggk[v] = cx(-(ee2[v] - ee1[v]), delt);
-      normal = chk1(a.dmna, a.dmnr, ggk).s == 0;
+      const Chk c = chk1(a.dmna, a.dmnr, ggk);
+      cat = c.s == 0 ? TC_NORMAL : c.s == 2 ? TC_S2 : c.s == 3 ? TC_S3
+          : c.s == 4 && c.i3 == 2 ? TC_S4A : c.s == 4 && c.i3 >= 3 && c.i3 <= 6 ? TC_S4B : TC_OTHER;
     }
-    if (normal) {
-      lists[atomicAdd(&n_normal, 1)] = t;
-    } else {
-      const int o = atomicAdd(&n_other, 2);
-      lists[2 * ntet - 1 - o] = 2 * t;
-      lists[2 * ntet - 2 - o] = 2 * t + 1;
+    tcat[t] = (unsigned char)cat;
+    if (cat != TC_SKIP) atomicAdd(&ncat[cat], 1);
+  }
+  __syncthreads();
+  // segments: the normal tetrahedra once (both signs in one pass), the others once per sign
+  if (threadIdx.x == 0) {
+    cbeg[0] = 0;
+    for (int c = 0; c < TC_NCAT; c++) {
+      cbeg[c + 1] = cbeg[c] + ncat[c] * (c == TC_NORMAL ? 1 : 2);
+      cur[c] = cbeg[c];
     }
   }
   __syncthreads();
+  for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
+    const int cat = tcat[t];
+    if (cat == TC_SKIP) continue;
+    if (cat == TC_NORMAL) {
+      lists[atomicAdd(&cur[cat], 1)] = t;
+    } else {
+      const int o = atomicAdd(&cur[cat], 2);
+      lists[o] = 2 * t;
+      lists[o + 1] = 2 * t + 1;
+    }
+  }
+  __syncthreads();
+  const int n_normal = ncat[TC_NORMAL];
   // normal tetrahedra: shared logs, real reciprocal differences, both signs
   for (int idx = threadIdx.x; idx < n_normal; idx += blockDim.x) {
     const int t = lists[idx];
@@ -615,9 +746,13 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
       for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], acc[v]);
     }
   }
-  // near-degenerate or Fermi-cut tetrahedra: the reference's forms
-  for (int idx = threadIdx.x; idx < n_other; idx += blockDim.x)
-    other_tetra(a, lists[2 * ntet - 1 - idx], e1m, e2m, Lt, e0, ne, nec, xo);
+  // near-degenerate tetrahedra, one category at a time so a warp runs one form
+  for (int cat = TC_S2; cat <= TC_S4B; cat++)
+    for (int idx = cbeg[cat] + threadIdx.x; idx < cbeg[cat + 1]; idx += blockDim.x)
+      degen_tetra(a, lists[idx], cat, e1m, e2m, Lt, e0, ne, nec, xo);
+  // Fermi-cut tetrahedra and unknown cases: the reference's ttct and forms
+  for (int idx = cbeg[TC_OTHER] + threadIdx.x; idx < cbeg[TC_OTHER + 1]; idx += blockDim.x)
+    other_tetra(a, lists[idx], e1m, e2m, Lt, e0, ne, nec, xo);
   __syncthreads();
   // w[(p*nen + e)*ntk + k] = xow(mesh(k), e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
   for (int i = threadIdx.x; i < ntk * ne; i += blockDim.x) {
@@ -635,7 +770,7 @@ int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st) {
   if (a.npair == 0) return 0;
   // weights (ntk x nec) and vertex logs (2 x ntk x nec) of a frequency chunk in shared memory
   int nec = a.nen;
-  const size_t fixed = 2 * sizeof(double) * (size_t)a.ntk + 2 * 6 * sizeof(int) * (size_t)a.ntk;
+  const size_t fixed = 2 * sizeof(double) * (size_t)a.ntk + 2 * 6 * sizeof(int) * (size_t)a.ntk + 6 * (size_t)a.ntk;
   const size_t budget = 210 * 1024 - fixed;
   while (nec > 1 && (size_t)a.ntk * nec * 3 * sizeof(double2) > budget) nec--;
   size_t smem = (size_t)a.ntk * nec * 3 * sizeof(double2) + fixed;
