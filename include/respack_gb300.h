@@ -147,6 +147,13 @@ long long rp_kernel_launches(const rp_ctx *ctx);
  * (task tables, Gamma rows, results fetched into host buffers). */
 int rp_transfer_bytes(const rp_ctx *ctx, long long *h2d, long long *d2h);
 
+/* 1 if the last rp_epsinv_q used the FP64 Gauss-Jordan inversion although the
+ * precision is a split (fast) one: the FP32 inverse had a zero pivot or a
+ * residual |I - eps X0|_F above 1e-3 in some matrix.  0 when the
+ * mixed-precision inverse (FP32 Gauss-Jordan plus one float-pair Newton step)
+ * was kept, and on the FP64 precision, which always inverts in FP64. */
+int rp_eps_fallback(const rp_ctx *ctx);
+
 const char *rp_last_error(const rp_ctx *ctx);
 void rp_ctx_destroy(rp_ctx *ctx);
 

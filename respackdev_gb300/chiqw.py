@@ -82,6 +82,8 @@ def load() -> C.CDLL:
     L.rp_kernel_launches.restype = C.c_longlong
     L.rp_transfer_bytes.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.rp_transfer_bytes.restype = C.c_int
+    L.rp_eps_fallback.argtypes = [vp]
+    L.rp_eps_fallback.restype = C.c_int
     L.rp_zinv_batched_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, vp]
     L.rp_zinv_batched_noalloc.restype = C.c_int
     L.rp_last_error.argtypes = [vp]
@@ -190,6 +192,10 @@ class Context:
 
     def kernel_launches(self) -> int:
         return int(self.L.rp_kernel_launches(self._h))
+
+    def eps_fallback(self) -> bool:
+        """True if the last epsinv_q fell back from the mixed-precision to the FP64 inversion."""
+        return bool(self.L.rp_eps_fallback(self._h))
 
     def transfer_bytes(self):
         """(host->device, device->host) bytes copied by this context's calls so far."""

@@ -68,12 +68,13 @@ struct rp_ctx {
   DevBuf coef, numirr, trs, src, phase, ng0, kg0, cfull, ur, energy, prob, imt1, index2, em, b9, sk0, errw;
   // per-q device data
   DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
-      rowcol, A, eps, prow, fcol, piv, used, intra, pwpl;
+      rowcol, A, eps, prow, fcol, piv, used, intra, pwpl, mixws, mixaux;
   rp::TcWorkspace tcw;
   rp::QTask task;
   int ndir = 1;
   double wd[3]{};
   bool have_chi = false, have_eps = false;
+  bool eps_fallback = false;  // the last rp_epsinv_q fell back to the FP64 inversion
   std::vector<cd> h_chi, h_eps;
   cudaEvent_t ev[6]{};
   double times[6]{};
@@ -82,7 +83,7 @@ struct rp_ctx {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
                       &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
-                      &intra, &pwpl})
+                      &intra, &pwpl, &mixws, &mixaux})
       b->release();
     tcw.release();
     for (auto &e : ev) if (e) cudaEventDestroy(e);
@@ -392,8 +393,32 @@ static void epsinv_run(rp_ctx *c) {
   for (int d = 0; d < 3; d++) a.wd[d] = c->wd[d];
   RP_CUDA(cudaEventRecord(c->ev[0], st));
   c->launches += rp::launch_eps_build(c->chi.as<double2>(), a, c->A.as<double2>(), st);
-  c->launches += rp::launch_gauss_jordan(c->A.as<double2>(), ng, nmat, c->prow.as<double2>(), c->fcol.as<double2>(),
-                                         c->piv.as<int>(), c->used.as<int>(), c->eps.as<double2>(), c->errw.as<int>(), st);
+  bool fp64 = c->S.params.precision == RP_PREC_FP64;
+  if (!fp64) {
+    // FP32 Gauss-Jordan plus one float-pair Newton step; its own singular flag and
+    // per-matrix |R|_F^2 decide whether the FP64 inversion has to run instead
+    c->mixws.ensure(rp::epsinv_mixed_bytes(ng, nmat));
+    c->mixaux.ensure(sizeof(float) * nmat + sizeof(int));
+    float *rn = c->mixaux.as<float>();
+    int *ferr = (int *)(rn + nmat);
+    RP_CUDA(cudaMemsetAsync(ferr, 0, sizeof(int), st));
+    c->launches += rp::launch_epsinv_mixed(c->A.as<double2>(), ng, nmat, c->mixws.p, c->piv.as<int>(),
+                                           c->used.as<int>(), c->eps.as<double2>(), rn, ferr, st);
+    std::vector<float> h(nmat + 1);
+    RP_CUDA(cudaMemcpyAsync(h.data(), rn, sizeof(float) * (nmat + 1), cudaMemcpyDeviceToHost, st));
+    RP_CUDA(cudaStreamSynchronize(st));
+    t_d2h += (long long)(sizeof(float) * (nmat + 1));
+    int fe;
+    std::memcpy(&fe, &h[nmat], sizeof(int));
+    bool ok = fe == 0;
+    for (int m = 0; m < nmat; m++) ok = ok && h[m] <= 1.0e-6f;  // |R|_F <= 1e-3, so |error| <~ 1e-6 |A^-1|
+    c->eps_fallback = !ok;
+    fp64 = !ok;
+  }
+  if (fp64)
+    c->launches += rp::launch_gauss_jordan(c->A.as<double2>(), ng, nmat, c->prow.as<double2>(), c->fcol.as<double2>(),
+                                           c->piv.as<int>(), c->used.as<int>(), c->eps.as<double2>(),
+                                           c->errw.as<int>(), st);
   RP_CUDA(cudaEventRecord(c->ev[1], st));
   check_device_error(c);
   float ms = 0;
@@ -544,6 +569,8 @@ int rp_q_dims(const rp_ctx *c, int iq, int *ng, int *ndir) {
 }
 
 long long rp_kernel_launches(const rp_ctx *c) { return c ? c->launches : 0; }
+
+int rp_eps_fallback(const rp_ctx *c) { return c && c->eps_fallback ? 1 : 0; }
 
 int rp_transfer_bytes(const rp_ctx *c, long long *h2d, long long *d2h) {
   if (!c) return 1;

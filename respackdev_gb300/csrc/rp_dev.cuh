@@ -124,6 +124,12 @@ struct EpsArgs {
 int launch_eps_build(const double2 *chi, const EpsArgs &a, double2 *A, cudaStream_t st);
 int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prow, double2 *fcol, int *piv, int *used,
                         double2 *out, int *err, cudaStream_t st);
+// Mixed-precision inverse of the nmat matrices A (n x n, column-major): FP32
+// Gauss-Jordan, a float-pair residual R = I - A X0 and one Newton step.
+// rnorm[m] receives |R|_F^2 of matrix m (device); ws holds epsinv_mixed_bytes.
+size_t epsinv_mixed_bytes(int n, int nmat);
+int launch_epsinv_mixed(const double2 *A, int n, int nmat, void *ws, int *piv, int *used, double2 *out,
+                        float *rnorm, int *err, cudaStream_t st);
 int launch_scale(double2 *x, size_t n, double divisor, cudaStream_t st);  // x /= divisor
 
 }  // namespace rp

@@ -106,7 +106,7 @@ def test_bad_input_reports_error(case_dir, fresh_copy):
 def test_chi0_tensor_core_matches_oracle(case_dir, fresh_copy, case, qs, prec, pair64):
     """Split-precision tcgen05 contraction: chi0 and eps^-1 within 1e-6 (normwise
     per frequency) of the FP64 oracle for the three-term FP16 split, with FP32
-    or FP64 pair densities."""
+    or FP64 pair densities; eps^-1 from the mixed-precision inverse."""
     if pair64 and prec != rp.PREC_FP16X3:
         pytest.skip("FP64 pair densities are checked with one split")
     kw = run_params(case)
@@ -119,6 +119,9 @@ def test_chi0_tensor_core_matches_oracle(case_dir, fresh_copy, case, qs, prec, p
             ref = orc.read_chi_dump(os.path.join(ref_root, "dir-eps", "q%03d" % iq, "dat.chi0"))
             worst = max(worst, normwise_err(chi, ref))
             eps = ctx.epsinv_q()
+            # the split precisions invert with the FP32 Gauss-Jordan plus one float-pair
+            # Newton step; these well-conditioned cases never need the FP64 fallback
+            assert not ctx.eps_fallback(), f"q{iq}: mixed-precision inverse fell back to FP64"
             ng, nen = eps.shape[0], eps.shape[2]
             er = read_eps_record(os.path.join(ref_root, "dir-eps", "q%03d" % iq, "dat.epsqw.600"), ng, nen)
             worst_eps = max(worst_eps, normwise_err(eps[..., 0], er))
