@@ -228,6 +228,30 @@ int rp_calc_j3d(const char *root, const char *namelist_text);
  * matrix) or -1 (CUDA error); rp_last_error(NULL) gives the text. */
 int rp_zinv_batched_noalloc(const double *a, double *ainv, int n, int nmat, void *stream);
 
+/* ---- band-tail MLP (no reference counterpart) ----------------------------
+ * A fully connected network nin -> nhid -> nhid -> nout (ReLU between layers)
+ * that predicts the chi0 contribution of the bands above a truncation per
+ * |q+G| shell (features and targets: respackdev_gb300/tail.py).  Trained and
+ * run on the GPU by the library's own kernels: FP32 master weights updated by
+ * Adam, a BF16 copy read by the forward and backward passes, FP32
+ * accumulation.  Loss: mean squared error over samples and outputs.  Arrays
+ * are host, row-major: x [n][nin], t and y [n][nout]; parameters in the order
+ * W1 [nhid][nin], b1 [nhid], W2 [nhid][nhid], b2 [nhid], W3 [nout][nhid],
+ * b3 [nout].  Sizes are at most 256.  Status codes as the calls above. */
+typedef struct rp_mlp rp_mlp;
+int rp_mlp_create(rp_mlp **out, int nin, int nhid, int nout, unsigned long long seed, int device);
+int rp_mlp_nparams(const rp_mlp *m);
+int rp_mlp_get_params(rp_mlp *m, float *params);
+int rp_mlp_set_params(rp_mlp *m, const float *params);   /* also resets Adam */
+int rp_mlp_forward(rp_mlp *m, const float *x, int n, float *y);
+/* loss and its gradient with respect to every parameter, for one batch */
+int rp_mlp_gradients(rp_mlp *m, const float *x, const float *t, int n, float *loss, float *grad);
+/* `steps` Adam steps on minibatches of `batch` samples taken in order
+ * (wrapping at n); losses[s] = minibatch loss before step s (may be NULL) */
+int rp_mlp_train(rp_mlp *m, const float *x, const float *t, int n, int steps, int batch, float lr, float *losses);
+const char *rp_mlp_last_error(const rp_mlp *m);
+void rp_mlp_destroy(rp_mlp *m);
+
 #ifdef __cplusplus
 }
 #endif
