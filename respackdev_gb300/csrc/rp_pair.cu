@@ -140,11 +140,13 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
 // the chunks of one k are consecutive in the grid, so the occupied bands of k
 // stay in L2 while every virtual band is read from HBM once.  Per z slab:
 //   pass 1 (y):  X[q][x][c2] = sum_y P_{2q}[x,y] TW2[y][c2], and the same for
-//                pair 2q+1 in the other half of the float4.  Thread (q, x)
-//                loads conj(u_vir) and both u_occ of its column from global
-//                memory (32 lanes = 32 consecutive x: coalesced) and keeps
-//                2 pairs x 16 frequencies in registers; the twiddle rows are
-//                warp-uniform (broadcast) 16-byte loads.
+//                pair 2q+1 in the other half of the float4.  Thread (pair, x)
+//                loads conj(u_vir) and u_occ of its column from global memory
+//                (32 lanes = 32 consecutive x: coalesced; u_vir shared in L1 by
+//                the chunk's pairs) and keeps up to 16 frequencies in
+//                registers; the twiddle rows are warp-uniform (broadcast)
+//                16-byte loads.  One pair per thread keeps the registers low
+//                enough for 18 warps per SM.
 //   pass 2 (x):  Y[j][c2][c1] = sum_x X[j][x][c2] TW1[x][c1], thread
 //                (q, tile) with a tile = (c2, group of 4 c1) holding at least
 //                one G of the sphere (about 30 of the 52 tiles of a 13x13
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
 //   z term:      acc[j][g] += Y[j][c2(g)][c1(g)] e^{-2 pi i f3(g) z / n3}.
 // Y and acc hold the two pairs of a couple side by side (float4), so the z
 // term moves both with one 16-byte access.
-constexpr int PD_THREADS = 160;
+constexpr int PD_THREADS = 288;  // one pass-1 row (pair, x) per thread for 8 pairs on a 36-point line
 constexpr int PD_CGMAX = 16;  // pass-1 output frequencies per register group, at most
 
 // pass-1 register group for D2 output frequencies: an even count (the twiddles
@@ -323,92 +325,85 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
     float2 *tz = TZ + (z & 1) * n3;
     for (int i = tid; i < n3; i += PD_THREADS) tz[i] = tw32((i * z) % n3, n3);
     if (pf && tid == 0 && z + 2 < n3) l2_prefetch_bulk(uvir + (size_t)(z + 2) * n12, (unsigned)(n12 * sizeof(float2)));
-    // pass 1: row = (couple q1, column x1); one row per thread when nq n1 <= PD_THREADS
-    for (int row = tid; row < nq * n1; row += PD_THREADS) {
-      const int q1 = row / n1, x1 = row - q1 * n1;
-      const int jA = 2 * q1, jB = min(2 * q1 + 1, cnt - 1);
+    // pass 1: row = (pair j1, column x1); one row per thread when cnt n1 <= PD_THREADS
+    for (int row = tid; row < cnt * n1; row += PD_THREADS) {
+      const int j1 = row / n1, x1 = row - j1 * n1;
       const float2 *pv = uvir + x1;
-      const float2 *pa = uocc + (size_t)a.pair_occ[a.pair_list[first + jA]] * bstride + x1;
-      const float2 *pb = uocc + (size_t)a.pair_occ[a.pair_list[first + jB]] * bstride + x1;
+      const float2 *pa = uocc + (size_t)a.pair_occ[a.pair_list[first + j1]] * bstride + x1;
       const size_t zo = (size_t)z * n12;
       for (int cg = 0; cg < D2; cg += CG) {
-        float2 sa[CG], sb[CG];
+        float2 sa[CG];
 #pragma unroll
-        for (int c = 0; c < CG; c++) { sa[c] = make_float2(0.f, 0.f); sb[c] = sa[c]; }
+        for (int c = 0; c < CG; c++) sa[c] = make_float2(0.f, 0.f);
         if (SPLIT) {
           // four rows (s a + b, a = 0..3) per step; the next step's rows in flight
-          float2 nv[4], na[4], nb[4];
+          float2 nv[4], na[4];
 #pragma unroll
           for (int u = 0; u < 4; u++) {
             const size_t o = zo + (size_t)(u * rows4) * n1;
-            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
+            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o);
           }
           for (int b = 0; b < rows4; b++) {
-            float2 PA[4], PB[4];
+            float2 PA[4];
             const int bn = min(b + 1, rows4 - 1);
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-              const float2 v = cmulc(nv[u], PH[u * rows4 + b]), va = na[u], vb = nb[u];
+              const float2 v = cmulc(nv[u], PH[u * rows4 + b]), va = na[u];
               const size_t o = zo + (size_t)(u * rows4 + bn) * n1;
-              nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
-              PA[u] = cmul(v, va); PB[u] = cmul(v, vb);
+              nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o);
+              PA[u] = cmul(v, va);
             }
-            float2 QA[4], QB[4];
+            float2 QA[4];
             bfly4(PA, QA);
-            bfly4(PB, QB);
             const float4 *t = (const float4 *)(TW2 + (size_t)b * L.D2P + cg);
 #pragma unroll
             for (int c = 0; c < CG / 2; c++) {
               const float4 w = t[c];
-              const float2 w0 = make_float2(w.x, w.y), w1 = make_float2(w.z, w.w);
-              cfma(sa[2 * c], QA[(2 * c) & 3], w0); cfma(sb[2 * c], QB[(2 * c) & 3], w0);
-              cfma(sa[2 * c + 1], QA[(2 * c + 1) & 3], w1); cfma(sb[2 * c + 1], QB[(2 * c + 1) & 3], w1);
+              cfma(sa[2 * c], QA[(2 * c) & 3], make_float2(w.x, w.y));
+              cfma(sa[2 * c + 1], QA[(2 * c + 1) & 3], make_float2(w.z, w.w));
             }
           }
         } else {
           const float4 *twr = (const float4 *)(TW2 + cg);
-          auto step = [&](float2 v, float2 va, float2 vb, int y) {
-          const float2 PA = cmulc(v, va), PB = cmulc(v, vb);
-          const float4 *t = twr + (size_t)y * (L.D2P / 2);
+          auto step = [&](float2 v, float2 va, int y) {
+            const float2 PA = cmulc(v, va);
+            const float4 *t = twr + (size_t)y * (L.D2P / 2);
 #pragma unroll
-          for (int c = 0; c < CG / 2; c++) {
-            const float4 w = t[c];
-            const float2 w0 = make_float2(w.x, w.y), w1 = make_float2(w.z, w.w);
-            cfma(sa[2 * c], PA, w0); cfma(sb[2 * c], PB, w0);
-            cfma(sa[2 * c + 1], PA, w1); cfma(sb[2 * c + 1], PB, w1);
-          }
-        };
-        // four rows in flight: each row's registers are refilled with the row
-        // four ahead as soon as they are consumed (row index clamped to the
-        // slab, so the loads need no guard)
-        const int n2f = n2 & ~3;
-        float2 nv[4], na[4], nb[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-          const size_t o = zo + (size_t)min(u, n2 - 1) * n1;
-          nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
-        }
-        for (int y0 = 0; y0 < n2f; y0 += 4) {
+            for (int c = 0; c < CG / 2; c++) {
+              const float4 w = t[c];
+              cfma(sa[2 * c], PA, make_float2(w.x, w.y));
+              cfma(sa[2 * c + 1], PA, make_float2(w.z, w.w));
+            }
+          };
+          // four rows in flight: each row's registers are refilled with the row
+          // four ahead as soon as they are consumed (row index clamped to the
+          // slab, so the loads need no guard)
+          const int n2f = n2 & ~3;
+          float2 nv[4], na[4];
 #pragma unroll
           for (int u = 0; u < 4; u++) {
-            const float2 cv = nv[u], ca = na[u], cb = nb[u];
-            const size_t o = zo + (size_t)min(y0 + 4 + u, n2 - 1) * n1;
-            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o); nb[u] = __ldg(pb + o);
-            step(cv, ca, cb, y0 + u);
+            const size_t o = zo + (size_t)min(u, n2 - 1) * n1;
+            nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o);
           }
-        }
+          for (int y0 = 0; y0 < n2f; y0 += 4) {
 #pragma unroll
-        for (int u = 0; u < 3; u++)
-          if (n2f + u < n2) step(nv[u], na[u], nb[u], n2f + u);
+            for (int u = 0; u < 4; u++) {
+              const float2 cv = nv[u], ca = na[u];
+              const size_t o = zo + (size_t)min(y0 + 4 + u, n2 - 1) * n1;
+              nv[u] = __ldg(pv + o); na[u] = __ldg(pa + o);
+              step(cv, ca, y0 + u);
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < 3; u++)
+            if (n2f + u < n2) step(nv[u], na[u], n2f + u);
         }
-        float4 *xr = X + (size_t)q1 * L.SQ + (size_t)x1 * L.D2X + cg;
+        // this pair's half of the couple's float4 (pair 2q in .xy, 2q + 1 in .zw)
+        float2 *xr = (float2 *)(X + (size_t)(j1 >> 1) * L.SQ + (size_t)x1 * L.D2X + cg) + (j1 & 1);
         const float2 ph1 = SPLIT ? PH1[x1] : make_float2(1.f, 0.f);
 #pragma unroll
         for (int c = 0; c < CG; c++)
-          if (cg + c < D2) {
-            const float2 va = SPLIT ? cmul(sa[c], ph1) : sa[c], vb = SPLIT ? cmul(sb[c], ph1) : sb[c];
-            xr[c] = make_float4(va.x, va.y, vb.x, vb.y);
-          }
+          if (cg + c < D2) xr[2 * c] = SPLIT ? cmul(sa[c], ph1) : sa[c];
       }
     }
     __syncthreads();
