@@ -222,10 +222,14 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
     for (int g = 0; g < ng; g++) r = std::max(r, std::abs(t.lg0[3 * g + d]));
     ep[d] = r;
   }
-  // pair batches sized so the per-batch buffers stay within a few GB
+  // pair batches: per pair the densities, weights and Gamma heads plus the
+  // contraction's operand rows, weights and three planes; one batch per q
+  // while that fits in 24 GB (the bench workload needs about 14 GB)
   const int npair = (int)t.pair_vir.size();
-  const size_t per_pair = (size_t)ntk * (ng * sizeof(cd) + nen * sizeof(cd) + 3 * sizeof(cd));
-  const size_t budget = (size_t)6 << 30;
+  const size_t per_pair = (size_t)ntk * (ng * sizeof(cd) + nen * sizeof(cd) + 3 * sizeof(cd) +
+                                         2 * (size_t)((ng + 127) / 128 * 128) * (sizeof(float) + 6) +
+                                         2 * (size_t)nen * 8);
+  const size_t budget = (size_t)24 << 30;
   int bsz = (int)std::max<size_t>(1, std::min<size_t>(npair, budget / std::max<size_t>(per_pair, 1)));
   // shared-memory limit of the pair-density tile decides how many pairs share one virtual band load
   int jmax = 8;
@@ -244,10 +248,28 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
     c->tcw.ksub = S.params.tc_ksub;
     rp::tc_begin_q(c->tcw, ng, nen, c->ndir, st);
   }
-  for (int p0 = 0; p0 < npair; p0 += bsz) {
-    const int nb = std::min(bsz, npair - p0);
-    std::vector<int> bv(t.pair_vir.begin() + p0, t.pair_vir.begin() + p0 + nb);
-    std::vector<int> bo(t.pair_occ.begin() + p0, t.pair_occ.begin() + p0 + nb);
+  // pairs grouped by virtual band (stable in the occupied band); a batch takes
+  // whole groups while they fit, so every pair-density chunk (pairs sharing a
+  // virtual band) is as full as jmax allows.  chi is a sum over pairs: the
+  // order changes only the rounding.
+  std::vector<int> ord(npair);
+  for (int i = 0; i < npair; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return t.pair_vir[a] < t.pair_vir[b]; });
+  std::vector<int> bstart{0};
+  for (int i = 0; i < npair;) {
+    int j = i;
+    while (j < npair && t.pair_vir[ord[j]] == t.pair_vir[ord[i]]) j++;  // group [i, j)
+    const int cur = i - bstart.back();
+    if (cur > 0 && cur + (j - i) > bsz) bstart.push_back(i);              // group starts a new batch
+    for (int s0 = i + bsz; s0 < j; s0 += bsz) bstart.push_back(s0);      // a group larger than a batch
+    i = j;
+  }
+  bstart.push_back(npair);
+  for (size_t bi = 0; bi + 1 < bstart.size(); bi++) {
+    const int p0 = bstart[bi], nb = bstart[bi + 1] - p0;
+    if (nb <= 0) continue;
+    std::vector<int> bv(nb), bo(nb);
+    for (int i = 0; i < nb; i++) { bv[i] = t.pair_vir[ord[p0 + i]]; bo[i] = t.pair_occ[ord[p0 + i]]; }
     std::vector<int> cv, cf, cc, pl;
     build_chunks(bv, bo, jmax, cv, cf, cc, pl);
     upload(c->pvir, bv, st);

@@ -39,6 +39,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "rp_dev.cuh"
@@ -125,11 +126,36 @@ __host__ __device__ constexpr uint32_t make_idesc(int bf16, int M, int N) {
          ((uint32_t)(M >> 4) << 24);
 }
 
+// COLL: the A operand's collector buffer -- 0 not kept, 1 fill (read A, keep
+// it), 2 use (the kept A, keep it), 3 last use (the kept A, release it).  The
+// products that share an A plane run back to back, so that plane is read from
+// shared memory once per K step instead of once per product.
+template <int COLL>
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-      "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  if (COLL == 1)
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  else if (COLL == 2)
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  else if (COLL == 3)
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  else
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+}
+// the collector mode of product pb of an A plane that has npb products
+template <int PB, int NPB>
+__device__ __forceinline__ void mma_plane(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
+  if (NPB == 1) mma_f16<0>(dtmem, ad, bd, idesc, accum);
+  else if (PB == 0) mma_f16<1>(dtmem, ad, bd, idesc, accum);
+  else if (PB == NPB - 1) mma_f16<3>(dtmem, ad, bd, idesc, accum);
+  else mma_f16<2>(dtmem, ad, bd, idesc, accum);
 }
 __device__ __forceinline__ void mma_commit(uint64_t *b) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
@@ -443,6 +469,45 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
       const uint32_t idesc = make_idesc(BF16 ? 1 : 0, BM, BN);
+      // descriptors of every plane tile of both stages, built once: per MMA the
+      // issuing thread only adds the K step (32 bytes = 2 units of the start
+      // address), since it shares its sub-partition with busy producer warps
+      uint64_t dA0[NP], dA1[NP], dB0[NP], dB1[NP];
+      const uint32_t sb0 = smem_u32(stage_base);
+#pragma unroll
+      for (int p = 0; p < NP; p++) {
+        dA0[p] = make_desc(sb0 + (uint32_t)(AOFF + p * TILE_BYTES));
+        dA1[p] = make_desc(sb0 + (uint32_t)(STAGE + AOFF + p * TILE_BYTES));
+        dB0[p] = make_desc(sb0 + (uint32_t)(BOFF + p * TILE_BYTES));
+        dB1[p] = make_desc(sb0 + (uint32_t)(STAGE + BOFF + p * TILE_BYTES));
+      }
+      // the MMAs of one K block in stage S: products of planes pa (A) and pb (B)
+      // with pa + pb <= NP - 1, grouped by A plane (collector reuse); with the
+      // exact scheme the leading product has its own accumulator.  The first
+      // product into each accumulator of a sub-chunk overwrites it.
+      auto issue = [&](auto S_, bool fresh_block) {
+        constexpr int S = decltype(S_)::value;
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; kk++) {
+          const bool fresh = fresh_block && kk == 0;
+          auto prod = [&](auto PA_, auto PB_) {
+            constexpr int pa = decltype(PA_)::value, pb = decltype(PB_)::value;
+            const uint64_t ad = (S == 0 ? dA0[pa] : dA1[pa]) + (uint64_t)(2 * kk);
+            const uint64_t bd = (S == 0 ? dB0[pb] : dB1[pb]) + (uint64_t)(2 * kk);
+            constexpr bool main_acc = (EXACT && pa == 0 && pb == 0) || !EXACT;
+            constexpr bool first = main_acc ? (pa == 0 && pb == 0) : (pa == 0 && pb == 1);
+            mma_plane<pb, NP - pa>(main_acc ? tmem : tmem + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
+          };
+          prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
+          prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
+          if constexpr (NP == 3) prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 2>{});
+          prod(std::integral_constant<int, 1>{}, std::integral_constant<int, 0>{});
+          if constexpr (NP == 3) {
+            prod(std::integral_constant<int, 1>{}, std::integral_constant<int, 1>{});
+            prod(std::integral_constant<int, 2>{}, std::integral_constant<int, 0>{});
+          }
+        }
+      };
       for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
         // the epilogue must have read the previous sub-chunk's sums
         if (sc > 0 && !mbar_wait(&accempty[0], (sc - 1) & 1, abort_flag)) break;
@@ -456,28 +521,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
             break;
           }
           tc_fence_after();
-          const uint32_t st = smem_u32(stage_base + (size_t)s * STAGE);
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; kk++) {
-            const bool fresh = (kb == kbeg && kk == 0);
-            int idx0 = 0, idx1 = 0;
-            // products of planes pa (A) and pb (B) with pa + pb <= NP - 1; with the
-            // exact scheme the leading product has its own accumulator
-#pragma unroll
-            for (int pa = 0; pa < NP; pa++)
-#pragma unroll
-              for (int pb = 0; pa + pb < NP; pb++) {
-                const uint64_t ad = make_desc(st + (uint32_t)(AOFF + pa * TILE_BYTES) + kk * 32);
-                const uint64_t bd = make_desc(st + (uint32_t)(BOFF + pb * TILE_BYTES) + kk * 32);
-                if ((EXACT && pa == 0 && pb == 0) || !EXACT) {
-                  mma_f16(tmem, ad, bd, idesc, (fresh && idx0 == 0) ? 0 : 1);
-                  idx0++;
-                } else {
-                  mma_f16(tmem + BN, ad, bd, idesc, (fresh && idx1 == 0) ? 0 : 1);
-                  idx1++;
-                }
-              }
-          }
+          if (s == 0) issue(std::integral_constant<int, 0>{}, kb == kbeg);
+          else issue(std::integral_constant<int, 1>{}, kb == kbeg);
           mma_commit(&empty[s]);
         }
         if (!ok) break;
