@@ -60,6 +60,8 @@ typedef struct rp_params {
                                   (as the reference) instead of FP32          */
   int    tc_ksub;              /* K blocks (of 64) per FP32 accumulation before
                                   the FP64 reduction (0 = default)            */
+  int    pair_batch;           /* at most this many band pairs per batch of a
+                                  q (0 = as many as fit in 24 GB)             */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */

@@ -231,6 +231,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
                                          2 * (size_t)nen * 8);
   const size_t budget = (size_t)24 << 30;
   int bsz = (int)std::max<size_t>(1, std::min<size_t>(npair, budget / std::max<size_t>(per_pair, 1)));
+  if (S.params.pair_batch > 0) bsz = std::min(bsz, S.params.pair_batch);
   // shared-memory limit of the pair-density tile decides how many pairs share one virtual band load
   int jmax = 8;
   const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];

@@ -1,0 +1,25 @@
+"""A q point split into several band-pair batches (pair_batch) gives the same
+chi0 and eps^-1 as one batch: batches take whole virtual-band groups, or split
+a group that is larger than the batch (pairs per virtual band = 4 here)."""
+from __future__ import annotations
+
+import pytest
+
+from respackdev_gb300 import chiqw as rp
+from tests.helpers import EM_TEST, normwise_err, run_params
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec,tol", [(rp.PREC_FP64, 1e-12), (rp.PREC_FP16X3, 1e-7)])
+def test_pair_batches_agree(case_dir, fresh_copy, prec, tol):
+    kw = run_params("tiny")
+    root = fresh_copy(case_dir("tiny"))
+    res = {}
+    for pb in (0, 5, 3):   # one batch; whole groups of 4; groups split 3 + 1
+        with rp.Context(root, rp.default_params(precision=prec, pair_batch=pb, **kw), EM_TEST) as ctx:
+            res[pb] = [(ctx.chi0_q(iq), ctx.epsinv_q()) for iq in (1, 2)]
+    for pb in (5, 3):
+        for (chi, eps), (chi0, eps0) in zip(res[pb], res[0]):
+            assert normwise_err(chi, chi0) < tol
+            assert normwise_err(eps, eps0) < tol
