@@ -148,9 +148,9 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
 //                16-byte loads.  One pair per thread keeps the registers low
 //                enough for 18 warps per SM.
 //   pass 2 (x):  Y[j][c2][c1] = sum_x X[j][x][c2] TW1[x][c1], thread
-//                (q, tile) with a tile = (c2, group of 4 c1) holding at least
-//                one G of the sphere (about 30 of the 52 tiles of a 13x13
-//                square); both pairs of the couple per load.
+//                (pair, tile) with a tile = (c2, group of 4 c1) holding at
+//                least one G of the sphere (about 30 of the 52 tiles of a
+//                13x13 square).
 //   z term:      acc[j][g] += Y[j][c2(g)][c1(g)] e^{-2 pi i f3(g) z / n3}.
 // Y and acc hold the two pairs of a couple side by side (float4), so the z
 // term moves both with one 16-byte access.
@@ -407,50 +407,45 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
       }
     }
     __syncthreads();
-    // pass 2: item = (q, tile)
+    // pass 2: item = (pair, tile); the pair's half of the couple's float4
     const int ntile = tlist[0];
-    for (int it = tid; it < ntile * nq; it += PD_THREADS) {
-      const int q = it / ntile, t = tlist[1 + it - q * ntile], grp = t / D2, cc2 = t - grp * D2;
-      float2 ya[4], yb[4];
+    for (int it = tid; it < ntile * cnt; it += PD_THREADS) {
+      const int j = it / ntile, t = tlist[1 + it - j * ntile], grp = t / D2, cc2 = t - grp * D2;
+      float2 ya[4];
 #pragma unroll
-      for (int c = 0; c < 4; c++) { ya[c] = make_float2(0.f, 0.f); yb[c] = ya[c]; }
-      const float4 *xc = X + (size_t)q * L.SQ + cc2;
+      for (int c = 0; c < 4; c++) ya[c] = make_float2(0.f, 0.f);
+      const float2 *xc = (const float2 *)(X + (size_t)(j >> 1) * L.SQ + cc2) + (j & 1);
       if (SPLIT) {
         // x = s a + b; residue r of c1 = 4 grp + r is r
         for (int b = 0; b < cols4; b++) {
-          float2 PA[4], PB[4];
+          float2 PA[4];
 #pragma unroll
-          for (int u = 0; u < 4; u++) {
-            const float4 v = xc[(size_t)(u * cols4 + b) * L.D2X];
-            PA[u] = make_float2(v.x, v.y); PB[u] = make_float2(v.z, v.w);
-          }
-          float2 QA[4], QB[4];
+          for (int u = 0; u < 4; u++) PA[u] = xc[2 * (size_t)(u * cols4 + b) * L.D2X];
+          float2 QA[4];
           bfly4(PA, QA);
-          bfly4(PB, QB);
           const float4 *tw = (const float4 *)(TW1 + (size_t)b * L.D1P + 4 * grp);
           const float4 t0 = tw[0], t1 = tw[1];
-          const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
-                               make_float2(t1.z, t1.w)};
-#pragma unroll
-          for (int c = 0; c < 4; c++) { cfma(ya[c], QA[c], w[c]); cfma(yb[c], QB[c], w[c]); }
+          cfma(ya[0], QA[0], make_float2(t0.x, t0.y));
+          cfma(ya[1], QA[1], make_float2(t0.z, t0.w));
+          cfma(ya[2], QA[2], make_float2(t1.x, t1.y));
+          cfma(ya[3], QA[3], make_float2(t1.z, t1.w));
         }
       } else {
         const float4 *tw = (const float4 *)(TW1 + 4 * grp);
 #pragma unroll 4
         for (int x = 0; x < n1; x++) {
-          const float4 v = xc[(size_t)x * L.D2X];
-          const float2 va = make_float2(v.x, v.y), vb = make_float2(v.z, v.w);
+          const float2 va = xc[2 * (size_t)x * L.D2X];
           const float4 t0 = tw[(size_t)x * (L.D1P / 2)], t1 = tw[(size_t)x * (L.D1P / 2) + 1];
-          const float2 w[4] = {make_float2(t0.x, t0.y), make_float2(t0.z, t0.w), make_float2(t1.x, t1.y),
-                               make_float2(t1.z, t1.w)};
-#pragma unroll
-          for (int c = 0; c < 4; c++) { cfma(ya[c], va, w[c]); cfma(yb[c], vb, w[c]); }
+          cfma(ya[0], va, make_float2(t0.x, t0.y));
+          cfma(ya[1], va, make_float2(t0.z, t0.w));
+          cfma(ya[2], va, make_float2(t1.x, t1.y));
+          cfma(ya[3], va, make_float2(t1.z, t1.w));
         }
       }
-      float4 *yq = Y + (size_t)q * D1 * D2 + (size_t)cc2 * D1 + 4 * grp;
+      float2 *yq = (float2 *)(Y + (size_t)(j >> 1) * D1 * D2 + (size_t)cc2 * D1 + 4 * grp) + (j & 1);
 #pragma unroll
       for (int c = 0; c < 4; c++)
-        if (4 * grp + c < D1) yq[c] = make_float4(ya[c].x, ya[c].y, yb[c].x, yb[c].y);
+        if (4 * grp + c < D1) yq[2 * c] = ya[c];
     }
     __syncthreads();
     // z term (overlaps the next slab's pass 1, which touches neither Y nor this tz)
