@@ -18,8 +18,12 @@
 // to nearest, so the products of integer leading terms go to their own
 // accumulator: their partial sums are integers below 2^24 over a sub-chunk of
 // up to 1024 K and stay exact; the five correction products, about 2^-7
-// smaller, go to a second accumulator.  After each sub-chunk the epilogue
-// warps add both, times the rows' scales, into an FP64 copy of the tile.
+// smaller, go to a second accumulator.  The accumulators are double-buffered
+// in tensor memory: while the tensor core fills one pair for sub-chunk s + 1,
+// the epilogue warps take sub-chunk s out of the other, unscale it (powers of
+// two: exact) and add it with TwoSum into a float-pair copy of the tile in
+// global memory (tile-blocked, rows contiguous, so a warp's 32 rows are one
+// coalesced access), converted to FP64 once when chi is assembled.
 //
 // Kernel layout: one CTA per (upper tile, frequency, Re/Im weight), 704 threads.
 //   warps 0-15  producers (8 rows each): read the FP32 rows of the A operand (prefetched one K
@@ -27,7 +31,7 @@
 //               planes and store them into shared memory in the 128-byte-swizzled
 //               K-major layout the tensor core reads;
 //   warps 16-19 epilogue: drain the FP32 accumulators from tensor memory
-//               (tcgen05.ld) into a float-pair running sum, then the FP64 tile;
+//               (tcgen05.ld) into the float-pair tile in global memory;
 //   warp 20     allocates tensor memory and issues tcgen05.mma (one thread);
 //   warp 21     loader (one thread): bulk-copies (cp.async.bulk) the B operand
 //               planes -- split once per batch by bplanes_kernel and shared by
@@ -70,7 +74,7 @@ struct TcArgs {
   int exact;              // 1: integer leading plane + separate accumulator
   const float2 *wt;       // [nen][Re/Im][Kp] weights as float pairs (hi, lo)
   const float *maxes;     // [0] = max|Y|, [1 + 2e] = max|Re w_e|, [2 + 2e] = max|Im w_e|
-  double *M64;            // [nen][2][Mp][Mp] FP64 tiles (upper triangle used)
+  float2 *Macc;           // float-pair tiles: [nen][2][ta][tb][col][row] (128 x 128 per tile, ta <= tb)
   int *err;
   int Mp, Kp, nen, ntile_side, ksub_blocks, nplanes, bf16;
   const int2 *tiles;      // (ta, tb) list, ta <= tb
@@ -162,43 +166,16 @@ __device__ __forceinline__ void mma_commit(uint64_t *b) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float *v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
-}
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
 #pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float *v) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-          taddr),
-      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
-      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
-      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])), "r"(__float_as_uint(v[15]))
-      : "memory");
+  for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // power-of-two scale that maps |v| <= vmax below 2^top (m 2^e -> m 2^top)
 __device__ __forceinline__ float scale_for(float vmax, int top) {
@@ -327,6 +304,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
   volatile int *abort_flag = (volatile int *)(bars + 15);
   uint32_t *tmem_slot = (uint32_t *)(bars + 16);
   float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
+  float *rB_s = sA_s + BM;                          // 1 / column scales of the B tile (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // channels vary fastest, so the CTAs running together share their operand rows in L2
@@ -360,7 +338,10 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   const int cidx = 2 * e + ch;
-  for (int i = tid; i < BM; i += NTHREADS) sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
+  for (int i = tid; i < BM; i += NTHREADS) {
+    sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
+    rB_s[i] = 1.0f / a.sB[tb * BN + i];  // exact: a power of two
+  }
   __syncthreads();
 
   if (warp < NPROD / 32) {
@@ -415,55 +396,42 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
       for (int i = 0; i < PROWS; i++) cur[i] = nxt[i];
     }
   } else if (warp < MMA_WARP) {
-    // ---------------- epilogue: fold each sub-chunk into a float-pair accumulator ----------------
-    // TMEM columns: [main][corr (exact scheme)][acc hi][acc lo], 128 each.
-    // acc = hi + lo is updated with an error-free TwoSum, so the running sum keeps
-    // about 48 bits with FP32 arithmetic only; the FP64 tile is written once.
+    // ---------------- epilogue: each sub-chunk into the float-pair tile ----------------
+    // TMEM columns: buffer b holds [main][corr (exact scheme)] at b * NACC * 128.
+    // The sub-chunk's sum (main exact, corr small) is unscaled by powers of two
+    // and added with an error-free TwoSum into (hi, lo) in global memory, so the
+    // running sum keeps about 48 bits with FP32 arithmetic only.
     const int q = warp & 3;                 // this warp may read TMEM lanes 32q..32q+31
-    const int row = ta * BM + 32 * q + lane;
+    const int rl = 32 * q + lane;           // row within the tile
     const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
-    const uint32_t cm = 0, cc = BN, chi = NACC * BN, clo = chi + BN;
+    const float ia = 1.0f / sA_s[rl];       // exact: a power of two
+    const int nt = a.ntile_side;
+    float2 *dst = a.Macc + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb) * BN) * BM + rl;  // + col * BM
     for (int sc = 0; sc < nsub; sc++) {
-      if (!mbar_wait(&accfull[0], sc & 1, abort_flag)) break;
+      const int b = sc & 1;
+      if (!mbar_wait(&accfull[b], (sc >> 1) & 1, abort_flag)) break;
       tc_fence_after();
+      const uint32_t base = lanebase + (uint32_t)(b * NACC * BN);
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        float m[16], cr[16], hi[16], lo[16];
-        tmem_ld16(lanebase + cm + c0, m);
-        if (NACC == 2) tmem_ld16(lanebase + cc + c0, cr);
-        if (sc > 0) { tmem_ld16(lanebase + chi + c0, hi); tmem_ld16(lanebase + clo + c0, lo); }
+      for (int c0 = 0; c0 < BN; c0 += 8) {
+        float2 g[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) g[j] = dst[(size_t)(c0 + j) * BM];
+        float m[8], cr[8];
+        tmem_ld8(base + c0, m);
+        if (NACC == 2) tmem_ld8(base + BN + c0, cr);
         tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const float a0 = sc > 0 ? hi[j] : 0.f, l0 = sc > 0 ? lo[j] : 0.f;
-          const float x = m[j];
-          const float sm = a0 + x, bb = sm - a0;
-          const float err = (a0 - (sm - bb)) + (x - bb);
-          hi[j] = sm;
-          lo[j] = l0 + err + (NACC == 2 ? cr[j] : 0.f);
+        for (int j = 0; j < 8; j++) {
+          const float f = ia * rB_s[c0 + j];
+          const float x = m[j] * f, l = (NACC == 2 ? cr[j] : 0.f) * f;
+          const float sm = g[j].x + x, bb = sm - g[j].x;
+          const float err = (g[j].x - (sm - bb)) + (x - bb);
+          dst[(size_t)(c0 + j) * BM] = make_float2(sm, g[j].y + err + l);
         }
-        tmem_st16(lanebase + chi + c0, hi);
-        tmem_st16(lanebase + clo + c0, lo);
       }
-      tmem_wait_st();
       tc_fence_before();
-      mbar_arrive(&accempty[0]);
-    }
-    // the batch's sum, unscaled, into the FP64 tile
-    if (!*abort_flag) {
-      tc_fence_after();
-      const double ia = 1.0 / (double)a.sA[(size_t)cidx * a.Mp + row];
-      double *dst = a.M64 + (((size_t)e * 2 + ch) * a.Mp + row) * a.Mp + tb * BN;
-      const float *sbc = a.sB + tb * BN;
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        float hi[16], lo[16];
-        tmem_ld16(lanebase + chi + c0, hi);
-        tmem_ld16(lanebase + clo + c0, lo);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 16; j++) dst[c0 + j] += ((double)hi[j] + (double)lo[j]) * ia / (double)sbc[c0 + j];
-      }
+      mbar_arrive(&accempty[b]);
     }
   } else if (warp == MMA_WARP) {
     if (lane == 0) {
@@ -485,7 +453,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
       // with pa + pb <= NP - 1, grouped by A plane (collector reuse); with the
       // exact scheme the leading product has its own accumulator.  The first
       // product into each accumulator of a sub-chunk overwrites it.
-      auto issue = [&](auto S_, bool fresh_block) {
+      auto issue = [&](auto S_, bool fresh_block, uint32_t tacc) {
         constexpr int S = decltype(S_)::value;
 #pragma unroll
         for (int kk = 0; kk < BK / 16; kk++) {
@@ -496,7 +464,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
             const uint64_t bd = (S == 0 ? dB0[pb] : dB1[pb]) + (uint64_t)(2 * kk);
             constexpr bool main_acc = (EXACT && pa == 0 && pb == 0) || !EXACT;
             constexpr bool first = main_acc ? (pa == 0 && pb == 0) : (pa == 0 && pb == 1);
-            mma_plane<pb, NP - pa>(main_acc ? tmem : tmem + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
+            mma_plane<pb, NP - pa>(main_acc ? tacc : tacc + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
           };
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
@@ -509,9 +477,11 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
         }
       };
       for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
-        // the epilogue must have read the previous sub-chunk's sums
-        if (sc > 0 && !mbar_wait(&accempty[0], (sc - 1) & 1, abort_flag)) break;
+        // accumulator pair b; the epilogue must have drained it (sub-chunk sc - 2)
+        const int b = sc & 1;
+        if (sc >= 2 && !mbar_wait(&accempty[b], ((sc - 2) >> 1) & 1, abort_flag)) break;
         tc_fence_after();
+        const uint32_t tacc = tmem + (uint32_t)(b * NACC * BN);
         const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
@@ -521,12 +491,12 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
             break;
           }
           tc_fence_after();
-          if (s == 0) issue(std::integral_constant<int, 0>{}, kb == kbeg);
-          else issue(std::integral_constant<int, 1>{}, kb == kbeg);
+          if (s == 0) issue(std::integral_constant<int, 0>{}, kb == kbeg, tacc);
+          else issue(std::integral_constant<int, 1>{}, kb == kbeg, tacc);
           mma_commit(&empty[s]);
         }
         if (!ok) break;
-        mma_commit(&accfull[0]);
+        mma_commit(&accfull[b]);
       }
       // wait for every MMA this thread issued before tensor memory is released
       mma_commit(fin);
@@ -700,17 +670,19 @@ __global__ void gamma_rowcol_f32_kernel(const float2 *__restrict__ rho, const do
   }
 }
 
-__device__ __forceinline__ double mget(const double *M, int Mp, int i, int j) {
-  // symmetric matrix stored in its upper tiles
-  const int ti = i / BM, tj = j / BN;
-  return ti <= tj ? M[(size_t)i * Mp + j] : M[(size_t)j * Mp + i];
+__device__ __forceinline__ double mget(const float2 *M, int nt, int i, int j) {
+  // symmetric matrix stored in its upper tiles (tile-blocked, rows contiguous), as float pairs
+  if (i / BM > j / BN) { const int t = i; i = j; j = t; }
+  const float2 v = M[(((size_t)(i / BM) * nt + j / BN) * BN + (j % BN)) * BM + (i % BM)];
+  return (double)v.x + (double)v.y;
 }
 
 // chi[e][g + ng h] = (Mr.rr + Mr.ii - Mi.ri + Mi.ir) + i (Mi.rr + Mi.ii + Mr.ri - Mr.ir)
-__global__ void assemble_kernel(const double *__restrict__ M64, int Mp, int Gp, int ng, int nen,
+__global__ void assemble_kernel(const float2 *__restrict__ Macc, int Mp, int Gp, int ng, int nen,
                                 double2 *__restrict__ chi) {
   const int e = blockIdx.y;
-  const double *Mr = M64 + ((size_t)e * 2 + 0) * Mp * Mp, *Mi = M64 + ((size_t)e * 2 + 1) * Mp * Mp;
+  const float2 *Mr = Macc + ((size_t)e * 2 + 0) * Mp * Mp, *Mi = Macc + ((size_t)e * 2 + 1) * Mp * Mp;
+  Mp = Mp / BM;  // tiles per side from here on
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (size_t)ng * ng;
        idx += (size_t)gridDim.x * blockDim.x) {
     const int g = (int)(idx % ng), h = (int)(idx / ng);
@@ -753,7 +725,7 @@ void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st) {
   ws.gram_seconds = 0;
   if (!ws.ev0) { RP_CUDA(cudaEventCreate(&ws.ev0)); RP_CUDA(cudaEventCreate(&ws.ev1)); }
   const int Mp = 2 * Gp_of(ng);
-  const size_t mbytes = sizeof(double) * (size_t)nen * 2 * Mp * Mp;
+  const size_t mbytes = sizeof(float2) * (size_t)nen * 2 * Mp * Mp;
   grow(ws.part, ws.part_bytes, mbytes);
   RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
 }
@@ -819,7 +791,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
     RP_CUDA(cudaGetLastError());
   }
   TcArgs a;
-  a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.M64 = (double *)ws.part; a.err = err;
+  a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.Macc = (float2 *)ws.part; a.err = err;
   a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;
   a.nplanes = nplanes;
   a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
@@ -831,7 +803,8 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
   a.tiles = (const int2 *)d_tiles;
   // per stage: A planes, B planes, the block's weights; then the barriers
-  const size_t smem = 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes * TILE_BYTES + 2 * (size_t)WBYTES + 256 + sizeof(float) * BM;
+  const size_t smem = 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes * TILE_BYTES + 2 * (size_t)WBYTES + 256 +
+                      2 * sizeof(float) * BM;
   if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
   void (*kern)(TcArgs);
   if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, true, false>;
@@ -855,7 +828,7 @@ int tc_end_q(TcWorkspace &ws, double2 *chi, double2 *rowcol, cudaStream_t st) {
   (void)rowcol;
   const int Gp = Gp_of(ws.ng), Mp = 2 * Gp;
   dim3 grid((unsigned)std::min<size_t>(((size_t)ws.ng * ws.ng + 255) / 256, 2048), ws.nen);
-  assemble_kernel<<<grid, 256, 0, st>>>((const double *)ws.part, Mp, Gp, ws.ng, ws.nen, chi);
+  assemble_kernel<<<grid, 256, 0, st>>>((const float2 *)ws.part, Mp, Gp, ws.ng, ws.nen, chi);
   RP_CUDA(cudaGetLastError());
   return 1;
 }
