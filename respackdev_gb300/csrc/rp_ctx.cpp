@@ -76,6 +76,8 @@ struct rp_ctx {
   bool have_chi = false, have_eps = false;
   bool eps_fallback = false;  // the last rp_epsinv_q fell back to the FP64 inversion
   std::vector<cd> h_chi, h_eps;
+  void *stage = nullptr;       // pinned two-slot staging buffer of device->host copies
+  cudaEvent_t sev[2]{};        // completion of each slot's copy
   cudaEvent_t ev[6]{};
   double times[6]{};
   long long h2d = 0, d2h = 0;  // bytes moved between host and device by this context's calls
@@ -87,6 +89,8 @@ struct rp_ctx {
       b->release();
     tcw.release();
     for (auto &e : ev) if (e) cudaEventDestroy(e);
+    for (auto &e : sev) if (e) cudaEventDestroy(e);
+    if (stage) cudaFreeHost(stage);
     if (st) cudaStreamDestroy(st);
   }
 };
@@ -450,12 +454,38 @@ static void epsinv_run(rp_ctx *c) {
   c->have_eps = true;
 }
 
+// Device -> host copy of `bytes` into any host memory: chunks go through two
+// pinned slots, so the host copy of chunk i out of its slot overlaps the
+// device copy of chunk i+1 into the other, and pageable destinations move at
+// pinned-copy speed.
+static void fetch_to(rp_ctx *c, const void *src, void *dst, size_t bytes) {
+  constexpr size_t CH = (size_t)8 << 20;
+  if (!c->stage) {
+    RP_CUDA(cudaMallocHost(&c->stage, 2 * CH));
+    for (auto &e : c->sev) RP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const size_t n = (bytes + CH - 1) / CH;
+  auto issue = [&](size_t i) {
+    const size_t o = i * CH, len = std::min(CH, bytes - o);
+    RP_CUDA(cudaMemcpyAsync((char *)c->stage + (i & 1) * CH, (const char *)src + o, len, cudaMemcpyDeviceToHost,
+                            c->st));
+    RP_CUDA(cudaEventRecord(c->sev[i & 1], c->st));
+  };
+  for (size_t i = 0; i < n && i < 2; i++) issue(i);
+  for (size_t i = 0; i < n; i++) {
+    RP_CUDA(cudaEventSynchronize(c->sev[i & 1]));
+    const size_t o = i * CH;
+    std::memcpy((char *)dst + o, (const char *)c->stage + (i & 1) * CH, std::min(CH, bytes - o));
+    if (i + 2 < n) issue(i + 2);
+  }
+  t_d2h += (long long)bytes;
+}
+
+static size_t result_elems(const rp_ctx *c) { return (size_t)c->ndir * c->S.em.size() * c->task.ng * c->task.ng; }
+
 static void fetch(rp_ctx *c, DevBuf &b, std::vector<cd> &h) {
-  const rp::QTask &t = c->task;
-  h.resize((size_t)c->ndir * c->S.em.size() * t.ng * t.ng);
-  RP_CUDA(cudaMemcpyAsync(h.data(), b.p, sizeof(cd) * h.size(), cudaMemcpyDeviceToHost, c->st));
-  RP_CUDA(cudaStreamSynchronize(c->st));
-  t_d2h += (long long)(sizeof(cd) * h.size());
+  h.resize(result_elems(c));
+  fetch_to(c, b.p, h.data(), sizeof(cd) * h.size());
 }
 
 static void mkdir_p(const std::string &p) { mkdir(p.c_str(), 0755); }
@@ -553,8 +583,7 @@ int rp_chi0_q(rp_ctx *c, int iq, double *chi, int *ng_out, int *ndir_out) {
     if (ng_out) *ng_out = c->task.ng;
     if (ndir_out) *ndir_out = c->ndir;
     if (chi) {
-      fetch(c, c->chi, c->h_chi);
-      std::memcpy(chi, c->h_chi.data(), sizeof(cd) * c->h_chi.size());
+      fetch_to(c, c->chi.p, chi, sizeof(cd) * result_elems(c));
     }
   });
 }
@@ -565,8 +594,7 @@ int rp_epsinv_q(rp_ctx *c, double *epsinv) {
     RP_CUDA(cudaSetDevice(c->dev));
     epsinv_run(c);
     if (epsinv) {
-      fetch(c, c->eps, c->h_eps);
-      std::memcpy(epsinv, c->h_eps.data(), sizeof(cd) * c->h_eps.size());
+      fetch_to(c, c->eps.p, epsinv, sizeof(cd) * result_elems(c));
     }
   });
 }

@@ -412,11 +412,17 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
       if (!mbar_wait(&accfull[b], (sc >> 1) & 1, abort_flag)) break;
       tc_fence_after();
       const uint32_t base = lanebase + (uint32_t)(b * NACC * BN);
+      // the running sums of the next 8 columns are loaded while these 8 are
+      // added, so each step waits for one global round trip less
+      float2 g[8], gn[8] = {};
+#pragma unroll
+      for (int j = 0; j < 8; j++) g[j] = dst[(size_t)j * BM];
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 8) {
-        float2 g[8];
+        if (c0 + 8 < BN) {
 #pragma unroll
-        for (int j = 0; j < 8; j++) g[j] = dst[(size_t)(c0 + j) * BM];
+          for (int j = 0; j < 8; j++) gn[j] = dst[(size_t)(c0 + 8 + j) * BM];
+        }
         float m[8], cr[8];
         tmem_ld8(base + c0, m);
         if (NACC == 2) tmem_ld8(base + BN + c0, cr);
@@ -428,6 +434,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
           const float sm = g[j].x + x, bb = sm - g[j].x;
           const float err = (g[j].x - (sm - bb)) + (x - bb);
           dst[(size_t)(c0 + j) * BM] = make_float2(sm, g[j].y + err + l);
+          g[j] = gn[j];
         }
       }
       tc_fence_before();
