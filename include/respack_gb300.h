@@ -62,6 +62,8 @@ typedef struct rp_params {
                                   the FP64 reduction (0 = default)            */
   int    pair_batch;           /* at most this many band pairs per batch of a
                                   q (0 = as many as fit in 24 GB)             */
+  int    tc_split;             /* K splits of the tensor-core Gram launch (0 =
+                                  measured per shape by the split tuner)      */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */
@@ -112,6 +114,28 @@ int rp_q_dims(const rp_ctx *ctx, int iq, int *ng, int *ndir);
  * and the contraction.  chi may be NULL (result stays on the device for
  * rp_epsinv_q).  ng_out / ndir_out report the sizes. */
 int rp_chi0_q(rp_ctx *ctx, int iq, double *chi, int *ng_out, int *ndir_out);
+
+/* chi0 of a ragged batch of problems: problem i is q point iqs[i] of context
+ * ctxs[i] (one cell per context; a context may appear several times, and the
+ * cells may differ in mesh, bands, G sphere and frequencies).  Every problem is
+ * prepared first (tetrahedron weights, pair densities, split operands); then
+ * ONE tensor-core Gram launch covers every (problem, tile, frequency, K split)
+ * of the batch, and it and the assembly of each problem's chi0 run as one CUDA
+ * graph (use_graph != 0) or as plain launches.  No reference counterpart: the
+ * reference computes one q at a time (chiqw.F:1264-1472 per q); each chi[i]
+ * (may be NULL) receives what rp_chi0_q(ctxs[i], iqs[i]) would give, up to the
+ * rounding of the K splits.  All contexts: one device, one tensor-core
+ * precision (not RP_PREC_FP64).  ng_out / ndir_out (may be NULL) get each
+ * problem's sizes; seconds (may be NULL) gets [preparation wall time, device
+ * time of the graph (Gram launch + assembly), finishing wall time].  The
+ * contexts have no current q afterwards (rp_epsinv_q needs rp_chi0_q). */
+int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, double *const *chi, int *ng_out,
+                  int *ndir_out, double *seconds);
+
+/* K-split shapes the tensor-core split tuner has measured in this process,
+ * and a reset of its cache (for tests). */
+int rp_tuned_shapes(void);
+void rp_reset_tuner(void);
 
 /* eps^-1(G,G',w) of the last rp_chi0_q: calc_eps_rpa / calc_eps_rpa_q_0 and
  * invZGE (chiqw_sub.F:386-568, invZGE.F90:1-22), FP64 on the device.

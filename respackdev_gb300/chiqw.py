@@ -35,7 +35,7 @@ class Params(C.Structure):
         ("n_calc_q", C.c_int), ("mpi_num_qcomm", C.c_int), ("precision", C.c_int), ("fft_box", C.c_int * 3),
         ("dump_chi", C.c_int), ("device", C.c_int), ("max_pairs", C.c_int), ("qshard_index", C.c_int),
         ("qshard_count", C.c_int), ("pair_fp64", C.c_int), ("tc_ksub", C.c_int),
-        ("pair_batch", C.c_int),
+        ("pair_batch", C.c_int), ("tc_split", C.c_int),
     ]
 
 
@@ -85,6 +85,10 @@ def load() -> C.CDLL:
     L.rp_transfer_bytes.restype = C.c_int
     L.rp_eps_fallback.argtypes = [vp]
     L.rp_eps_fallback.restype = C.c_int
+    L.rp_chi0_batch.argtypes = [C.POINTER(vp), ip, C.c_int, C.c_int, C.POINTER(vp), ip, ip, dp]
+    L.rp_chi0_batch.restype = C.c_int
+    L.rp_tuned_shapes.restype = C.c_int
+    L.rp_reset_tuner.restype = None
     L.rp_zinv_batched_noalloc.argtypes = [vp, vp, C.c_int, C.c_int, vp]
     L.rp_zinv_batched_noalloc.restype = C.c_int
     L.rp_last_error.argtypes = [vp]
@@ -243,3 +247,45 @@ def plan_q(root: str, namelist_text: str) -> list:
     if rc:
         raise RuntimeError(f"rp_plan_q failed ({rc}): {L.rp_last_error(None).decode()}")
     return list(buf[: min(n.value, cap)])
+
+
+def chi0_batch(problems: Sequence, graph: bool = True, fetch: bool = True):
+    """chi0 of a ragged batch: problems is a list of (Context, iq).  Every
+    problem is prepared, then one tensor-core launch covers them all (inside a
+    CUDA graph when graph is true).  Returns (list of chi0 arrays shaped like
+    Context.chi0_q's, or None when fetch is false; seconds
+    [preparation, graph device time, finishing])."""
+    L = load()
+    n = len(problems)
+    if n == 0:
+        return [], np.zeros(3)
+    ctxs = (C.c_void_p * n)(*[c._h.value for c, _ in problems])
+    iqs = (C.c_int * n)(*[int(iq) for _, iq in problems])
+    outs, ptrs = [], (C.c_void_p * n)()
+    if fetch:
+        for i, (c, iq) in enumerate(problems):
+            ng, nd = c.q_dims(iq)
+            a = np.empty(nd * c.info().nen * ng * ng, dtype=np.complex128)
+            outs.append(a)
+            ptrs[i] = a.ctypes.data
+    ngo, ndo = (C.c_int * n)(), (C.c_int * n)()
+    sec = (C.c_double * 3)()
+    rc = L.rp_chi0_batch(ctxs, iqs, n, 1 if graph else 0, ptrs if fetch else None, ngo, ndo, sec)
+    if rc:
+        raise RuntimeError(f"rp_chi0_batch failed ({rc}): {L.rp_last_error(problems[0][0]._h).decode()}")
+    res = None
+    if fetch:
+        res = []
+        for i, (c, _) in enumerate(problems):
+            ng, nd, nen = ngo[i], ndo[i], c.info().nen
+            res.append(outs[i].reshape(nd, nen, ng, ng).transpose(3, 2, 1, 0))
+    return res, np.array(sec[:])
+
+
+def tuned_shapes() -> int:
+    """Shapes the tensor-core K-split tuner has measured in this process."""
+    return int(load().rp_tuned_shapes())
+
+
+def reset_tuner() -> None:
+    load().rp_reset_tuner()

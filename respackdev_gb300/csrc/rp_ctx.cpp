@@ -11,6 +11,7 @@
 #include <sys/stat.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -200,36 +201,53 @@ static void build_chunks(const std::vector<int> &pvir, const std::vector<int> &p
   (void)pocc;
 }
 
-static void chi0_q(rp_ctx *c, int iq, bool fast) {
+// One q point while its chi0 is computed: the task, where chi0 accumulates,
+// the pair batches and the stage timings.  The single-q path keeps these in
+// the context; a ragged batch (rp_chi0_batch) keeps one per problem.
+struct QRun {
+  int iq = 0;
+  bool fast = false;
+  rp::QTask *t = nullptr;
+  DevBuf *chi = nullptr, *rowcol = nullptr;
+  int ndir = 1, ng = 0, nen = 0, ntk = 0, jmax = 8, npair = 0;
+  int ep[3]{};
+  std::vector<int> ord, bstart;
+  float tms[4]{};
+};
+
+static void upload_qtables(rp_ctx *c, const rp::QTask &t) {
+  upload(c->kpq, t.kpq, c->st);
+  upload(c->shift, t.shift, c->st);
+  upload(c->lg0, t.lg0, c->st);
+  upload(c->qglen, t.qglen, c->st);
+}
+
+// Tables of the q, chi0 zeroed, the pair batches planned.
+static void q_begin(rp_ctx *c, QRun &r) {
   rp::Setup &S = c->S;
   cudaStream_t st = c->st;
-  c->have_chi = c->have_eps = false;
-  c->task = rp::make_qtask(S, iq - 1, S.params.max_pairs);
-  rp::QTask &t = c->task;
-  c->ndir = t.gamma ? 3 : 1;
-  const int ng = t.ng, nen = (int)S.em.size(), ntk = S.ntk;
-  upload(c->kpq, t.kpq, st);
-  upload(c->shift, t.shift, st);
-  upload(c->lg0, t.lg0, st);
-  upload(c->qglen, t.qglen, st);
+  rp::QTask &t = *r.t;
+  r.ndir = t.gamma ? 3 : 1;
+  r.ng = t.ng; r.nen = (int)S.em.size(); r.ntk = S.ntk;
+  const int ng = r.ng, nen = r.nen, ntk = r.ntk;
+  upload_qtables(c, t);
   RP_CUDA(cudaMemsetAsync(c->errw.p, 0, 16, st));
-  const size_t chisz = (size_t)c->ndir * nen * ng * ng;
-  c->chi.ensure(sizeof(cd) * chisz);
-  RP_CUDA(cudaMemsetAsync(c->chi.p, 0, sizeof(cd) * chisz, st));
+  const size_t chisz = (size_t)r.ndir * nen * ng * ng;
+  r.chi->ensure(sizeof(cd) * chisz);
+  RP_CUDA(cudaMemsetAsync(r.chi->p, 0, sizeof(cd) * chisz, st));
   if (t.gamma) {
-    c->rowcol.ensure(sizeof(cd) * 4 * (size_t)nen * ng);
-    RP_CUDA(cudaMemsetAsync(c->rowcol.p, 0, sizeof(cd) * 4 * (size_t)nen * ng, st));
+    r.rowcol->ensure(sizeof(cd) * 4 * (size_t)nen * ng);
+    RP_CUDA(cudaMemsetAsync(r.rowcol->p, 0, sizeof(cd) * 4 * (size_t)nen * ng, st));
   }
-  int ep[3];
   for (int d = 0; d < 3; d++) {
-    int r = 0;
-    for (int g = 0; g < ng; g++) r = std::max(r, std::abs(t.lg0[3 * g + d]));
-    ep[d] = r;
+    int m = 0;
+    for (int g = 0; g < ng; g++) m = std::max(m, std::abs(t.lg0[3 * g + d]));
+    r.ep[d] = m;
   }
   // pair batches: per pair the densities, weights and Gamma heads plus the
   // contraction's operand rows, weights and three planes; one batch per q
   // while that fits in 24 GB (the bench workload needs about 14 GB)
-  const int npair = (int)t.pair_vir.size();
+  const int npair = r.npair = (int)t.pair_vir.size();
   const size_t per_pair = (size_t)ntk * (ng * sizeof(cd) + nen * sizeof(cd) + 3 * sizeof(cd) +
                                          2 * (size_t)((ng + 127) / 128 * 128) * (sizeof(float) + 6) +
                                          2 * (size_t)nen * 8);
@@ -238,120 +256,140 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   if (S.params.pair_batch > 0) bsz = std::min(bsz, S.params.pair_batch);
   // shared-memory limit of the pair-density tile decides how many pairs share one virtual band load
   int jmax = 8;
-  const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];
   auto smem_of = [&](int j, size_t elt) {
     rp::PairGeom gq;
-    gq.n1 = n1; gq.n2 = n2; gq.n3 = n3; gq.R1 = ep[0]; gq.R2 = ep[1]; gq.ng = ng;
+    gq.n1 = S.nw[0]; gq.n2 = S.nw[1]; gq.n3 = S.nw[2]; gq.R1 = r.ep[0]; gq.R2 = r.ep[1]; gq.ng = ng;
     return rp::pair_density_smem(gq, j, elt == sizeof(double) * 2);
   };
-  const size_t elt = (fast && !S.params.pair_fp64) ? sizeof(float) * 2 : sizeof(double) * 2;
+  const size_t elt = (r.fast && !S.params.pair_fp64) ? sizeof(float) * 2 : sizeof(double) * 2;
   while (jmax > 1 && smem_of(jmax, elt) > 220 * 1024) jmax--;
   if (smem_of(jmax, elt) > 220 * 1024) rp::fail(1, "dielectric sphere (NG=%d) too large for the pair-density tile", ng);
-  float tms[4] = {0, 0, 0, 0};
-  RP_CUDA(cudaEventRecord(c->ev[5], st));
-  if (fast) {
-    c->tcw.ksub = S.params.tc_ksub;
-    rp::tc_begin_q(c->tcw, ng, nen, c->ndir, st);
-  }
+  r.jmax = jmax;
   // pairs grouped by virtual band (stable in the occupied band); a batch takes
   // whole groups while they fit, so every pair-density chunk (pairs sharing a
   // virtual band) is as full as jmax allows.  chi is a sum over pairs: the
   // order changes only the rounding.
-  std::vector<int> ord(npair);
-  for (int i = 0; i < npair; i++) ord[i] = i;
-  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return t.pair_vir[a] < t.pair_vir[b]; });
-  std::vector<int> bstart{0};
+  r.ord.resize(npair);
+  for (int i = 0; i < npair; i++) r.ord[i] = i;
+  std::stable_sort(r.ord.begin(), r.ord.end(), [&](int a, int b) { return t.pair_vir[a] < t.pair_vir[b]; });
+  r.bstart.assign(1, 0);
   for (int i = 0; i < npair;) {
     int j = i;
-    while (j < npair && t.pair_vir[ord[j]] == t.pair_vir[ord[i]]) j++;  // group [i, j)
-    const int cur = i - bstart.back();
-    if (cur > 0 && cur + (j - i) > bsz) bstart.push_back(i);              // group starts a new batch
-    for (int s0 = i + bsz; s0 < j; s0 += bsz) bstart.push_back(s0);      // a group larger than a batch
+    while (j < npair && t.pair_vir[r.ord[j]] == t.pair_vir[r.ord[i]]) j++;  // group [i, j)
+    const int cur = i - r.bstart.back();
+    if (cur > 0 && cur + (j - i) > bsz) r.bstart.push_back(i);              // group starts a new batch
+    for (int s0 = i + bsz; s0 < j; s0 += bsz) r.bstart.push_back(s0);      // a group larger than a batch
     i = j;
   }
-  bstart.push_back(npair);
-  for (size_t bi = 0; bi + 1 < bstart.size(); bi++) {
-    const int p0 = bstart[bi], nb = bstart[bi + 1] - p0;
-    if (nb <= 0) continue;
-    std::vector<int> bv(nb), bo(nb);
-    for (int i = 0; i < nb; i++) { bv[i] = t.pair_vir[ord[p0 + i]]; bo[i] = t.pair_occ[ord[p0 + i]]; }
-    std::vector<int> cv, cf, cc, pl;
-    build_chunks(bv, bo, jmax, cv, cf, cc, pl);
-    upload(c->pvir, bv, st);
-    upload(c->pocc, bo, st);
-    upload(c->chunk_vir, cv, st);
-    upload(c->chunk_first, cf, st);
-    upload(c->chunk_count, cc, st);
-    upload(c->pair_list, pl, st);
-    // tetrahedron weights
-    rp::TetraArgs ta;
-    ta.ntk = ntk; ta.nen = nen; ta.ntb = S.ntb; ta.imt1 = c->imt1.as<int>(); ta.index_kpt = c->index2.as<int>();
-    ta.numirr = c->numirr.as<int>(); ta.kpq = c->kpq.as<int>(); ta.energy = c->energy.as<double>();
-    ta.prob = c->prob.as<double2>(); ta.em = c->em.as<double2>(); ta.pair_vir = c->pvir.as<int>();
-    ta.pair_occ = c->pocc.as<int>(); ta.npair = nb; ta.efermi = S.efermi; ta.delt = S.delt; ta.dmna = S.dmna;
-    ta.dmnr = S.dmnr; ta.err = c->errw.as<int>();
-    c->wts.ensure(sizeof(cd) * (size_t)nb * nen * ntk);
-    RP_CUDA(cudaEventRecord(c->ev[0], st));
-    c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st);
-    RP_CUDA(cudaEventRecord(c->ev[1], st));
-    rp::PairGeom pg;
-    pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;
-    pg.kpq = c->kpq.as<int>(); pg.shift = c->shift.as<int>(); pg.lg0 = c->lg0.as<int>();
-    pg.R1 = ep[0]; pg.R2 = ep[1]; pg.R3 = ep[2];
-    rp::PairChunks pc;
-    pc.chunk_vir = c->chunk_vir.as<int>(); pc.chunk_first = c->chunk_first.as<int>();
-    pc.chunk_count = c->chunk_count.as<int>(); pc.pair_list = c->pair_list.as<int>();
-    pc.pair_occ = c->pocc.as<int>(); pc.nchunk = (int)cv.size(); pc.jmax = jmax;
-    if (t.gamma) {
-      c->head.ensure(sizeof(cd) * 3 * (size_t)nb * ntk);
-      c->launches += rp::launch_gamma_head(c->cfull.as<double2>(), c->ng0.as<int>(), c->kg0.as<int>(), ntk, S.ncb,
-                                           S.ntg, c->b9.as<double>(), c->energy.as<double>(), S.ntb,
-                                           c->numirr.as<int>(), c->pvir.as<int>(), c->pocc.as<int>(), nb, S.delt,
-                                           c->head.as<double2>(), st);
-    }
-    if (!fast) {
-      c->rho.ensure(sizeof(cd) * (size_t)nb * ntk * ng);
-      c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
-      RP_CUDA(cudaEventRecord(c->ev[2], st));
-      if (t.gamma) {
-        c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
-                                               ntk, ng, nen, t.no_g0, c->rowcol.as<double2>(), st);
-        c->launches += rp::launch_set_head(c->rho.as<double2>(), c->head.as<double2>(), nb, ntk, ng, t.no_g0, 0, st);
-      }
-      c->launches += rp::launch_contract_fp64(c->rho.as<double2>(), c->wts.as<double2>(), nb, ntk, ng, nen,
-                                              c->chi.as<double2>(), st);
-    } else {
-      const bool p64 = S.params.pair_fp64 != 0;
-      c->rho.ensure((p64 ? sizeof(cd) : sizeof(float) * 2) * (size_t)nb * ntk * ng);
-      if (p64) c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
-      else c->launches += rp::launch_pair_density_fp32(c->ur.as<float2>(), pg, pc, c->rho.as<float2>(), st);
-      RP_CUDA(cudaEventRecord(c->ev[2], st));
-      if (p64 && t.gamma)
-        c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
-                                               ntk, ng, nen, t.no_g0, c->rowcol.as<double2>(), st);
-      c->launches += rp::tc_contract_batch(c->tcw, p64 ? nullptr : c->rho.as<float2>(),
-                                           p64 ? c->rho.as<double2>() : nullptr, c->wts.as<double2>(),
-                                           t.gamma ? c->head.as<double2>() : nullptr, nb, ntk, ng, nen, t.no_g0,
-                                           S.params.precision, c->chi.as<double2>(),
-                                           t.gamma ? c->rowcol.as<double2>() : nullptr, c->errw.as<int>(), st);
-    }
-    RP_CUDA(cudaEventRecord(c->ev[3], st));
-    RP_CUDA(cudaEventSynchronize(c->ev[3]));
-    float a = 0, b = 0, d = 0;
-    RP_CUDA(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
-    RP_CUDA(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
-    RP_CUDA(cudaEventElapsedTime(&d, c->ev[2], c->ev[3]));
-    tms[0] += a; tms[1] += b; tms[2] += d;
+  r.bstart.push_back(npair);
+  for (float &x : r.tms) x = 0;
+}
+
+static int q_nbatch(const QRun &r) { return (int)r.bstart.size() - 1; }
+static int q_batch_pairs(const QRun &r, int bi) { return r.bstart[bi + 1] - r.bstart[bi]; }
+
+// Pair batch bi: tetrahedron weights, pair densities and the contraction.  With
+// run_gram false (tensor-core precisions only) the batch is prepared in ws and
+// its Gram launch is left to the caller.
+static void q_batch(rp_ctx *c, QRun &r, int bi, rp::TcWorkspace *ws, bool run_gram) {
+  rp::Setup &S = c->S;
+  cudaStream_t st = c->st;
+  rp::QTask &t = *r.t;
+  const int ng = r.ng, nen = r.nen, ntk = r.ntk;
+  const int n1 = S.nw[0], n2 = S.nw[1], n3 = S.nw[2];
+  const int p0 = r.bstart[bi], nb = r.bstart[bi + 1] - p0;
+  if (nb <= 0) return;
+  std::vector<int> bv(nb), bo(nb);
+  for (int i = 0; i < nb; i++) { bv[i] = t.pair_vir[r.ord[p0 + i]]; bo[i] = t.pair_occ[r.ord[p0 + i]]; }
+  std::vector<int> cv, cf, cc, pl;
+  build_chunks(bv, bo, r.jmax, cv, cf, cc, pl);
+  upload(c->pvir, bv, st);
+  upload(c->pocc, bo, st);
+  upload(c->chunk_vir, cv, st);
+  upload(c->chunk_first, cf, st);
+  upload(c->chunk_count, cc, st);
+  upload(c->pair_list, pl, st);
+  // tetrahedron weights
+  rp::TetraArgs ta;
+  ta.ntk = ntk; ta.nen = nen; ta.ntb = S.ntb; ta.imt1 = c->imt1.as<int>(); ta.index_kpt = c->index2.as<int>();
+  ta.numirr = c->numirr.as<int>(); ta.kpq = c->kpq.as<int>(); ta.energy = c->energy.as<double>();
+  ta.prob = c->prob.as<double2>(); ta.em = c->em.as<double2>(); ta.pair_vir = c->pvir.as<int>();
+  ta.pair_occ = c->pocc.as<int>(); ta.npair = nb; ta.efermi = S.efermi; ta.delt = S.delt; ta.dmna = S.dmna;
+  ta.dmnr = S.dmnr; ta.err = c->errw.as<int>();
+  c->wts.ensure(sizeof(cd) * (size_t)nb * nen * ntk);
+  RP_CUDA(cudaEventRecord(c->ev[0], st));
+  c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st);
+  RP_CUDA(cudaEventRecord(c->ev[1], st));
+  rp::PairGeom pg;
+  pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;
+  pg.kpq = c->kpq.as<int>(); pg.shift = c->shift.as<int>(); pg.lg0 = c->lg0.as<int>();
+  pg.R1 = r.ep[0]; pg.R2 = r.ep[1]; pg.R3 = r.ep[2];
+  rp::PairChunks pc;
+  pc.chunk_vir = c->chunk_vir.as<int>(); pc.chunk_first = c->chunk_first.as<int>();
+  pc.chunk_count = c->chunk_count.as<int>(); pc.pair_list = c->pair_list.as<int>();
+  pc.pair_occ = c->pocc.as<int>(); pc.nchunk = (int)cv.size(); pc.jmax = r.jmax;
+  if (t.gamma) {
+    c->head.ensure(sizeof(cd) * 3 * (size_t)nb * ntk);
+    c->launches += rp::launch_gamma_head(c->cfull.as<double2>(), c->ng0.as<int>(), c->kg0.as<int>(), ntk, S.ncb,
+                                         S.ntg, c->b9.as<double>(), c->energy.as<double>(), S.ntb,
+                                         c->numirr.as<int>(), c->pvir.as<int>(), c->pocc.as<int>(), nb, S.delt,
+                                         c->head.as<double2>(), st);
   }
-  if (fast) c->launches += rp::tc_end_q(c->tcw, c->chi.as<double2>(), t.gamma ? c->rowcol.as<double2>() : nullptr, st);
+  double2 *chi = r.chi->as<double2>();
+  double2 *rowcol = t.gamma ? r.rowcol->as<double2>() : nullptr;
+  if (!r.fast) {
+    c->rho.ensure(sizeof(cd) * (size_t)nb * ntk * ng);
+    c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
+    RP_CUDA(cudaEventRecord(c->ev[2], st));
+    if (t.gamma) {
+      c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
+                                             ntk, ng, nen, t.no_g0, rowcol, st);
+      c->launches += rp::launch_set_head(c->rho.as<double2>(), c->head.as<double2>(), nb, ntk, ng, t.no_g0, 0, st);
+    }
+    c->launches += rp::launch_contract_fp64(c->rho.as<double2>(), c->wts.as<double2>(), nb, ntk, ng, nen, chi, st);
+  } else {
+    const bool p64 = S.params.pair_fp64 != 0;
+    c->rho.ensure((p64 ? sizeof(cd) : sizeof(float) * 2) * (size_t)nb * ntk * ng);
+    if (p64) c->launches += rp::launch_pair_density_fp64(c->ur.as<float2>(), pg, pc, c->rho.as<double2>(), st);
+    else c->launches += rp::launch_pair_density_fp32(c->ur.as<float2>(), pg, pc, c->rho.as<float2>(), st);
+    RP_CUDA(cudaEventRecord(c->ev[2], st));
+    if (p64 && t.gamma)
+      c->launches += rp::launch_gamma_rowcol(c->rho.as<double2>(), c->wts.as<double2>(), c->head.as<double2>(), nb,
+                                             ntk, ng, nen, t.no_g0, rowcol, st);
+    const float2 *rho32 = p64 ? nullptr : c->rho.as<float2>();
+    const double2 *rho64 = p64 ? c->rho.as<double2>() : nullptr;
+    const double2 *head = t.gamma ? c->head.as<double2>() : nullptr;
+    if (run_gram)
+      c->launches += rp::tc_contract_batch(*ws, rho32, rho64, c->wts.as<double2>(), head, nb, ntk, ng, nen, t.no_g0,
+                                           S.params.precision, chi, rowcol, c->errw.as<int>(), st);
+    else
+      c->launches += rp::tc_prepare(*ws, rho32, rho64, c->wts.as<double2>(), head, nb, ntk, ng, nen, t.no_g0,
+                                    S.params.precision, rowcol, c->errw.as<int>(), st);
+  }
+  RP_CUDA(cudaEventRecord(c->ev[3], st));
+  RP_CUDA(cudaEventSynchronize(c->ev[3]));
+  float a = 0, b = 0, d = 0;
+  RP_CUDA(cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+  RP_CUDA(cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+  RP_CUDA(cudaEventElapsedTime(&d, c->ev[2], c->ev[3]));
+  r.tms[0] += a; r.tms[1] += b; r.tms[2] += d;
+}
+
+// Gamma's directions 2 and 3, the 1/VOLUME scale and the Drude term.
+static void q_end(rp_ctx *c, QRun &r) {
+  rp::Setup &S = c->S;
+  cudaStream_t st = c->st;
+  rp::QTask &t = *r.t;
+  const int ng = r.ng, nen = r.nen, ntk = r.ntk;
+  const size_t chisz = (size_t)r.ndir * nen * ng * ng;
   // Gamma: directions 2 and 3 share the body of direction 1 and get their own G=0 row/column
   if (t.gamma) {
     const size_t m = (size_t)nen * ng * ng;
-    double2 *chi = c->chi.as<double2>();
+    double2 *chi = r.chi->as<double2>();
     RP_CUDA(cudaMemcpyAsync(chi + m, chi, sizeof(cd) * m, cudaMemcpyDeviceToDevice, st));
     RP_CUDA(cudaMemcpyAsync(chi + 2 * m, chi, sizeof(cd) * m, cudaMemcpyDeviceToDevice, st));
     std::vector<cd> rc(4 * (size_t)nen * ng);
-    RP_CUDA(cudaMemcpyAsync(rc.data(), c->rowcol.p, sizeof(cd) * rc.size(), cudaMemcpyDeviceToHost, st));
+    RP_CUDA(cudaMemcpyAsync(rc.data(), r.rowcol->p, sizeof(cd) * rc.size(), cudaMemcpyDeviceToHost, st));
     t_d2h += (long long)(sizeof(cd) * rc.size());
     RP_CUDA(cudaStreamSynchronize(st));
     for (int ix = 1; ix <= 2; ix++)
@@ -368,10 +406,11 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
         RP_CUDA(cudaStreamSynchronize(st));
       }
   }
-  c->launches += rp::launch_scale(c->chi.as<double2>(), chisz, S.volume, st);
+  c->launches += rp::launch_scale(r.chi->as<double2>(), chisz, S.volume, st);
   // Drude plasma frequency from the intraband pairs (metals, fRPA only)
   c->wd[0] = c->wd[1] = c->wd[2] = 0;
   if (t.gamma && !t.intra_band.empty()) {
+    upload_qtables(c, t);  // another q of this context may have replaced them (ragged batches)
     upload(c->intra, t.intra_band, st);
     c->pwpl.ensure(sizeof(cd) * 3);
     RP_CUDA(cudaMemsetAsync(c->pwpl.p, 0, sizeof(cd) * 3, st));
@@ -395,9 +434,28 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   }
   RP_CUDA(cudaEventRecord(c->ev[4], st));
   check_device_error(c);
+}
+
+static void chi0_q(rp_ctx *c, int iq, bool fast) {
+  rp::Setup &S = c->S;
+  c->have_chi = c->have_eps = false;
+  c->task = rp::make_qtask(S, iq - 1, S.params.max_pairs);
+  QRun r;
+  r.iq = iq; r.fast = fast; r.t = &c->task; r.chi = &c->chi; r.rowcol = &c->rowcol;
+  q_begin(c, r);
+  c->ndir = r.ndir;
+  RP_CUDA(cudaEventRecord(c->ev[5], c->st));
+  if (fast) {
+    c->tcw.ksub = S.params.tc_ksub;
+    rp::tc_begin_q(c->tcw, r.ng, r.nen, r.ndir, S.params.tc_split, (long)r.npair * r.ntk, S.params.precision, c->st);
+  }
+  for (int bi = 0; bi < q_nbatch(r); bi++) q_batch(c, r, bi, &c->tcw, true);
+  if (fast) c->launches += rp::tc_end_q(c->tcw, c->chi.as<double2>(), nullptr, c->st);
+  q_end(c, r);
   float tot = 0;
   RP_CUDA(cudaEventElapsedTime(&tot, c->ev[5], c->ev[4]));
-  c->times[0] = tms[0] * 1e-3; c->times[1] = tms[1] * 1e-3; c->times[2] = tms[2] * 1e-3; c->times[4] = tot * 1e-3;
+  c->times[0] = r.tms[0] * 1e-3; c->times[1] = r.tms[1] * 1e-3; c->times[2] = r.tms[2] * 1e-3;
+  c->times[4] = tot * 1e-3;
   c->times[5] = fast ? c->tcw.gram_seconds : 0.0;
   c->have_chi = true;
 }
@@ -587,6 +645,85 @@ int rp_chi0_q(rp_ctx *c, int iq, double *chi, int *ng_out, int *ndir_out) {
     }
   });
 }
+
+int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, double *const *chi, int *ng_out,
+                  int *ndir_out, double *seconds) {
+  if (!ctxs || !iqs || n <= 0 || !ctxs[0]) return 1;
+  rp_ctx *c0 = ctxs[0];
+  return guarded(c0, [&] {
+    struct Prob {
+      rp_ctx *c = nullptr;
+      rp::QTask task;
+      DevBuf chi, rowcol;
+      QRun r;
+      std::vector<std::unique_ptr<rp::TcWorkspace>> ws;
+      ~Prob() {
+        chi.release();
+        rowcol.release();
+        for (auto &w : ws) w->release();
+      }
+    };
+    const int prec = c0->S.params.precision;
+    if (prec == RP_PREC_FP64) rp::fail(1, "rp_chi0_batch needs a tensor-core precision");
+    for (int i = 0; i < n; i++) {
+      rp_ctx *c = ctxs[i];
+      if (!c) rp::fail(1, "rp_chi0_batch: context %d is NULL", i);
+      if (c->dev != c0->dev) rp::fail(1, "rp_chi0_batch: contexts on different devices");
+      if (c->S.params.precision != prec) rp::fail(1, "rp_chi0_batch: contexts with different precisions");
+      if (iqs[i] < 1 || iqs[i] > c->S.nk_irr) rp::fail(1, "q index %d outside dat.sample-k (1..%d)", iqs[i], c->S.nk_irr);
+    }
+    RP_CUDA(cudaSetDevice(c0->dev));
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    std::vector<std::unique_ptr<Prob>> P;
+    for (int i = 0; i < n; i++) {
+      rp_ctx *c = ctxs[i];
+      auto p = std::make_unique<Prob>();
+      p->c = c;
+      c->have_chi = c->have_eps = false;
+      p->task = rp::make_qtask(c->S, iqs[i] - 1, c->S.params.max_pairs);
+      p->r.iq = iqs[i]; p->r.fast = true; p->r.t = &p->task; p->r.chi = &p->chi; p->r.rowcol = &p->rowcol;
+      q_begin(c, p->r);
+      for (int bi = 0; bi < q_nbatch(p->r); bi++) {
+        auto ws = std::make_unique<rp::TcWorkspace>();
+        ws->ksub = c->S.params.tc_ksub;
+        rp::tc_begin_q(*ws, p->r.ng, p->r.nen, p->r.ndir, c->S.params.tc_split,
+                       (long)q_batch_pairs(p->r, bi) * p->r.ntk, prec, c->st);
+        p->ws.push_back(std::move(ws));
+        q_batch(c, p->r, bi, p->ws.back().get(), false);
+      }
+      check_device_error(c);
+      P.push_back(std::move(p));
+    }
+    const auto t1 = clk::now();
+    // one grouped Gram launch over every prepared batch, then each batch into its problem's chi
+    std::vector<rp::TcWorkspace *> wl;
+    std::vector<double2 *> cl;
+    for (auto &p : P)
+      for (auto &w : p->ws)
+        if (w->ready) { wl.push_back(w.get()); cl.push_back(p->chi.as<double2>()); }
+    const double gsec = rp::tc_group_run(wl.data(), (int)wl.size(), cl.data(), c0->errw.as<int>(), c0->st,
+                                         use_graph != 0, &c0->launches);
+    check_device_error(c0);
+    const auto t2 = clk::now();
+    for (int i = 0; i < n; i++) {
+      Prob &p = *P[i];
+      q_end(p.c, p.r);
+      if (ng_out) ng_out[i] = p.r.ng;
+      if (ndir_out) ndir_out[i] = p.r.ndir;
+      if (chi && chi[i]) fetch_to(p.c, p.chi.p, chi[i], sizeof(cd) * (size_t)p.r.ndir * p.r.nen * p.r.ng * p.r.ng);
+    }
+    const auto t3 = clk::now();
+    if (seconds) {
+      seconds[0] = std::chrono::duration<double>(t1 - t0).count();
+      seconds[1] = gsec;
+      seconds[2] = std::chrono::duration<double>(t3 - t2).count();
+    }
+  });
+}
+
+int rp_tuned_shapes(void) { return rp::tc_tuned_shapes(); }
+void rp_reset_tuner(void) { rp::tc_reset_tuner(); }
 
 int rp_epsinv_q(rp_ctx *c, double *epsinv) {
   if (!c) return 1;

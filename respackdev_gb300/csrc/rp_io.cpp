@@ -287,6 +287,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "pair_fp64") p->pair_fp64 = nl_int(v, k);
       else if (k == "tc_ksub") p->tc_ksub = nl_int(v, k);
       else if (k == "pair_batch") p->pair_batch = nl_int(v, k);
+      else if (k == "tc_split") p->tc_split = nl_int(v, k);
       else if (k == "freq_re_ev") for (auto &x : v) fre.push_back(to_num(x));
       else if (k == "freq_im_ev") for (auto &x : v) fim.push_back(to_num(x));
       else fail(1, "namelist &param_gpu: unknown name '%s'", k.c_str());

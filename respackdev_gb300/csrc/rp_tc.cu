@@ -43,6 +43,9 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 #include <vector>
 
@@ -67,18 +70,27 @@ constexpr int WCHUNK = 16;                 // K blocks per weight chunk
 constexpr int WBYTES = WCHUNK * BK * 8;    // one channel's weights of a chunk (float2 per K)
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
+// One problem of a (possibly ragged) group: a prepared pair batch of one q.
 struct TcArgs {
   const float *Yt;        // [Mp][Kp] rows: Re rho (0..Gp), Im rho (Gp..2Gp)
   const float *sB;        // [Mp] row scales of the unweighted operand
   const float *sA;        // [2 nen][Mp] row scales of the weighted operand per channel
-  int exact;              // 1: integer leading plane + separate accumulator
   const float2 *wt;       // [nen][Re/Im][Kp] weights as float pairs (hi, lo)
-  const float *maxes;     // [0] = max|Y|, [1 + 2e] = max|Re w_e|, [2 + 2e] = max|Im w_e|
-  float2 *Macc;           // float-pair tiles: [nen][2][ta][tb][col][row] (128 x 128 per tile, ta <= tb)
-  int *err;
-  int Mp, Kp, nen, ntile_side, ksub_blocks, nplanes, bf16;
-  const int2 *tiles;      // (ta, tb) list, ta <= tb
+  // float-pair tiles, one slice per K split: [split][nen][2][ta][tb][col][row]
+  // (128 x 128 per tile, ta <= tb); `slice` elements per split
+  float2 *Macc;
   const unsigned char *Bp;  // B operand planes, [tb][kb][plane] tiles of TILE_BYTES
+  size_t slice;
+  int Mp, Kp, nen, ntile_side, ksub_blocks;
+  int kb_split;           // K blocks per split (the last split takes the rest)
+};
+
+// A grouped launch: CTA i takes work item work[i] = (problem, ta | tb << 16,
+// channel 2e + Re/Im, split).
+struct TcGroup {
+  const TcArgs *probs;
+  const int4 *work;
+  int *err;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -287,10 +299,12 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 // NP operand planes, EXACT integer leading plane, BF16 or FP16.  One CTA per
-// (upper tile, frequency, Re/Im weight); see the file comment for the roles.
+// work item (problem, upper tile, frequency, Re/Im weight, K split); see the
+// file comment for the roles.
 template <int NP, bool EXACT, bool BF16>
 // 22 warps: at most 6 on one SM sub-partition, whose 16K registers allow 85 per thread
-__global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
+__global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
+  __shared__ TcArgs sh_args;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
@@ -307,14 +321,18 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
   float *rB_s = sA_s + BM;                          // 1 / column scales of the B tile (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // channels vary fastest, so the CTAs running together share their operand rows in L2
-  const int e = blockIdx.x >> 1, ch = blockIdx.x & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
-  const int2 tt = a.tiles[blockIdx.y];
-  const int ta = tt.x, tb = tt.y;
-  const int nkb = a.Kp / BK;
-  const int nsub = (nkb + a.ksub_blocks - 1) / a.ksub_blocks;
+  // the work list has channels fastest, so the CTAs running together share their operand rows in L2
+  const int4 wk = grp.work[blockIdx.x];
+  const TcArgs &a = sh_args;
+  const int ta = wk.y & 0xffff, tb = wk.y >> 16;
+  const int cidx = wk.z, e = cidx >> 1, ch = cidx & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
+  {
+    const TcArgs &p = grp.probs[wk.x];
+    if (wk.w * p.kb_split >= p.Kp / BK) return;  // empty K range (the host makes none): the whole CTA leaves
+  }
 
   if (tid == 0) {
+    sh_args = grp.probs[wk.x];
     for (int s = 0; s < NSTAGE; s++) {
       mbar_init(&full[s], NPROD);
       mbar_init(&bfull[s], 1);
@@ -337,7 +355,11 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int cidx = 2 * e + ch;
+  // this CTA's K range: blocks kb0 .. kb0 + nkb - 1 of the problem
+  const int nkb_all = a.Kp / BK, kb0 = wk.w * a.kb_split;
+  const int nkb = min(nkb_all - kb0, a.kb_split);
+  const int ksub = a.ksub_blocks;
+  const int nsub = (nkb + ksub - 1) / ksub;
   for (int i = tid; i < BM; i += NTHREADS) {
     sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
     rB_s[i] = 1.0f / a.sB[tb * BN + i];  // exact: a power of two
@@ -351,7 +373,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
     // the lane's two weights serve all the warp's rows, and each plane store writes one
     // full 128-byte swizzled row.
     const int pw = warp, r0 = PROWS * pw;
-    const float2 *ya = (const float2 *)(a.Yt + (size_t)(ta * BM + r0) * a.Kp) + lane;
+    const float2 *ya = (const float2 *)(a.Yt + (size_t)(ta * BM + r0) * a.Kp + (size_t)kb0 * BK) + lane;
     const size_t rstride = (size_t)a.Kp / 2;  // float2 per row
     float2 cur[PROWS], nxt[PROWS];
 #pragma unroll
@@ -406,7 +428,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
     const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
     const float ia = 1.0f / sA_s[rl];       // exact: a power of two
     const int nt = a.ntile_side;
-    float2 *dst = a.Macc + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb) * BN) * BM + rl;  // + col * BM
+    float2 *dst = a.Macc + (size_t)wk.w * a.slice + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb) * BN) * BM +
+                  rl;  // + col * BM
     for (int sc = 0; sc < nsub; sc++) {
       const int b = sc & 1;
       if (!mbar_wait(&accfull[b], (sc >> 1) & 1, abort_flag)) break;
@@ -489,7 +512,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
         if (sc >= 2 && !mbar_wait(&accempty[b], ((sc - 2) >> 1) & 1, abort_flag)) break;
         tc_fence_after();
         const uint32_t tacc = tmem + (uint32_t)(b * NACC * BN);
-        const int kbeg = sc * a.ksub_blocks, kend = min(nkb, kbeg + a.ksub_blocks);
+        const int kbeg = sc * ksub, kend = min(nkb, kbeg + ksub);
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
           const int s = kb & 1, use = kb >> 1;
@@ -511,8 +534,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
     }
   } else if (lane == 0) {
     // ---------------- loader: B planes per K block, weights per chunk, by bulk copy ----------------
-    const unsigned char *bsrc = a.Bp + (size_t)tb * nkb * NP * TILE_BYTES;
-    const float2 *wsrc = a.wt + (size_t)cidx * a.Kp;
+    const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES;
+    const float2 *wsrc = a.wt + (size_t)cidx * a.Kp + (size_t)kb0 * BK;
     const int nchunk = (nkb + WCHUNK - 1) / WCHUNK;
     auto issue_w = [&](int c) {
       const uint32_t bytes = (uint32_t)min(WCHUNK, nkb - c * WCHUNK) * BK * 8;
@@ -548,7 +571,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcArgs a) {
     }
   }
   __syncwarp();
-  if (tid == 0 && *abort_flag) atomicExch(a.err, 4);
+  if (tid == 0 && *abort_flag) atomicExch(grp.err, 4);
   tc_fence_before();
   __syncthreads();
   if (warp == MMA_WARP) {
@@ -677,26 +700,32 @@ __global__ void gamma_rowcol_f32_kernel(const float2 *__restrict__ rho, const do
   }
 }
 
-__device__ __forceinline__ double mget(const float2 *M, int nt, int i, int j) {
-  // symmetric matrix stored in its upper tiles (tile-blocked, rows contiguous), as float pairs
+// element (i, j) of a symmetric matrix stored in its upper tiles (tile-blocked,
+// rows contiguous) as float pairs, summed over the K-split slices
+__device__ __forceinline__ double mget(const float2 *M, size_t slice, int nslice, int nt, int i, int j) {
   if (i / BM > j / BN) { const int t = i; i = j; j = t; }
-  const float2 v = M[(((size_t)(i / BM) * nt + j / BN) * BN + (j % BN)) * BM + (i % BM)];
-  return (double)v.x + (double)v.y;
+  const size_t o = (((size_t)(i / BM) * nt + j / BN) * BN + (j % BN)) * BM + (i % BM);
+  double v = 0;
+  for (int s = 0; s < nslice; s++) {
+    const float2 x = M[s * slice + o];
+    v += (double)x.x + (double)x.y;
+  }
+  return v;
 }
 
-// chi[e][g + ng h] = (Mr.rr + Mr.ii - Mi.ri + Mi.ir) + i (Mi.rr + Mi.ii + Mr.ri - Mr.ir)
-__global__ void assemble_kernel(const float2 *__restrict__ Macc, int Mp, int Gp, int ng, int nen,
+// chi[e][g + ng h] += (Mr.rr + Mr.ii - Mi.ri + Mi.ir) + i (Mi.rr + Mi.ii + Mr.ri - Mr.ir)
+__global__ void assemble_kernel(const float2 *__restrict__ Macc, size_t slice, int nslice, int Mp, int Gp, int ng,
                                 double2 *__restrict__ chi) {
   const int e = blockIdx.y;
   const float2 *Mr = Macc + ((size_t)e * 2 + 0) * Mp * Mp, *Mi = Macc + ((size_t)e * 2 + 1) * Mp * Mp;
-  Mp = Mp / BM;  // tiles per side from here on
+  const int nt = Mp / BM;
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (size_t)ng * ng;
        idx += (size_t)gridDim.x * blockDim.x) {
     const int g = (int)(idx % ng), h = (int)(idx / ng);
-    const double rr_r = mget(Mr, Mp, g, h), ii_r = mget(Mr, Mp, Gp + g, Gp + h);
-    const double ri_r = mget(Mr, Mp, g, Gp + h), ir_r = mget(Mr, Mp, Gp + g, h);
-    const double rr_i = mget(Mi, Mp, g, h), ii_i = mget(Mi, Mp, Gp + g, Gp + h);
-    const double ri_i = mget(Mi, Mp, g, Gp + h), ir_i = mget(Mi, Mp, Gp + g, h);
+    const double rr_r = mget(Mr, slice, nslice, nt, g, h), ii_r = mget(Mr, slice, nslice, nt, Gp + g, Gp + h);
+    const double ri_r = mget(Mr, slice, nslice, nt, g, Gp + h), ir_r = mget(Mr, slice, nslice, nt, Gp + g, h);
+    const double rr_i = mget(Mi, slice, nslice, nt, g, h), ii_i = mget(Mi, slice, nslice, nt, Gp + g, Gp + h);
+    const double ri_i = mget(Mi, slice, nslice, nt, g, Gp + h), ir_i = mget(Mi, slice, nslice, nt, Gp + g, h);
     double2 *d = chi + (size_t)e * ng * ng + idx;
     d->x += rr_r + ii_r - ri_i + ir_i;
     d->y += rr_i + ii_i + ri_r - ir_r;
@@ -725,28 +754,235 @@ static void *grow(void *&p, size_t &have, size_t need) {
   return p;
 }
 
-static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
 
-void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, cudaStream_t st) {
-  ws.ng = ng; ws.nen = nen; ws.ndir = ndir;
-  ws.gram_seconds = 0;
-  if (!ws.ev0) { RP_CUDA(cudaEventCreate(&ws.ev0)); RP_CUDA(cudaEventCreate(&ws.ev1)); }
-  const int Mp = 2 * Gp_of(ng);
-  const size_t mbytes = sizeof(float2) * (size_t)nen * 2 * Mp * Mp;
-  grow(ws.part, ws.part_bytes, mbytes);
-  RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
+static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
+static int nplanes_of(int precision) { return (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2; }
+static size_t smem_of(int precision) {
+  // per stage: A planes, B planes; the weight ring; then the barriers and the scales
+  return 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes_of(precision) * TILE_BYTES + 2 * (size_t)WBYTES + 256 +
+         2 * sizeof(float) * BM;
+}
+static size_t slice_of(int Mp, int nen) { return (size_t)nen * 2 * Mp * Mp; }
+// K blocks per FP32 sub-chunk: 1024 K by default; the integer leading plane's
+// partial sums stay exact (below 2^24) only up to that length
+static int ksub_of(const TcWorkspace &ws) {
+  const int k = ws.ksub > 0 ? ws.ksub : 16;
+  return nplanes_of(ws.precision) == 3 ? std::min(k, 16) : k;
 }
 
-int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const double2 *w, const double2 *head,
-                      int npair, int ntk, int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol,
-                      int *err, cudaStream_t st) {
-  (void)chi;
+// ---------------------------------------------------------------------------
+// K-split tuner.  A q point whose upper tiles x channels give fewer than two
+// CTAs per SM leaves SMs idle; splitting K across CTAs (each split into its
+// own float-pair slice, summed when chi is assembled) fills them at the cost
+// of more sums to drain.  The best split of a shape (precision, Mp, nen, K
+// order of magnitude) is measured once on the first batch of that shape and
+// cached for the process.
+
+namespace {
+constexpr int SPLIT_MAX = 16;
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tuned;
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    RP_CUDA(cudaGetDevice(&dev));
+    RP_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return n;
+}
+int kbits(long nkb) {
+  int b = 0;
+  while ((2L << b) <= nkb) b++;
+  return b;
+}
+// K blocks per split for `split` splits of nkb blocks: whole sub-chunks
+int kb_split_of(int nkb, int split, int ksub) {
+  int per = (nkb + split - 1) / split;
+  per = ((per + ksub - 1) / ksub) * ksub;
+  return std::max(per, 1);
+}
+}  // namespace
+
+int tc_tuned_shapes() {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  return (int)g_tuned.size();
+}
+void tc_reset_tuner() {
+  std::lock_guard<std::mutex> g(g_tune_mu);
+  g_tuned.clear();
+}
+
+void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, int split_req, long k_estimate, int precision,
+                cudaStream_t st) {
+  ws.ng = ng; ws.nen = nen; ws.ndir = ndir;
+  ws.gram_seconds = 0;
+  ws.ready = 0;
+  if (!ws.ev0) { RP_CUDA(cudaEventCreate(&ws.ev0)); RP_CUDA(cudaEventCreate(&ws.ev1)); }
+  const int Mp = 2 * Gp_of(ng), nt = Mp / BM;
+  const long nkb = std::max(1L, (k_estimate + BK - 1) / BK);
+  const long ctas = (long)nt * (nt + 1) / 2 * 2 * nen;
+  ws.tune_pending = 0;
+  ws.precision = precision;
+  if (split_req > 0) {
+    ws.nsplit = std::min(split_req, SPLIT_MAX);
+  } else if (ctas >= 2L * num_sms() || nkb < 2L * ksub_of(ws)) {
+    ws.nsplit = 1;
+  } else {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    auto it = g_tuned.find(std::make_tuple(precision, Mp, nen, kbits(nkb)));
+    if (it != g_tuned.end()) {
+      ws.nsplit = it->second;
+    } else {
+      ws.nsplit = 1;
+      ws.tune_pending = 1;
+    }
+  }
+  ws.nslice = ws.tune_pending ? SPLIT_MAX : ws.nsplit;
+  const size_t mbytes = sizeof(float2) * slice_of(Mp, nen) * ws.nslice;
+  grow(ws.part, ws.part_bytes, mbytes);
+  RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
+  ws.precision = precision;
+  ws.Mp = Mp;
+  ws.Kp = (int)(nkb * BK);  // the tuner's key until a batch is prepared
+}
+
+// ---------------------------------------------------------------------------
+// grouped launch
+
+namespace {
+struct GroupScratch {
+  void *dev = nullptr;
+  size_t bytes = 0;
+};
+thread_local GroupScratch g_scratch;
+
+// The problem table and the work list of a group, uploaded to `dev`.
+struct GroupPlan {
+  const TcArgs *probs = nullptr;
+  const int4 *work = nullptr;
+  int nwork = 0, precision = 0;
+  size_t smem = 0;
+};
+
+GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev, size_t &have) {
+  GroupPlan P;
+  if (n <= 0) return P;
+  P.precision = wss[0]->precision;
+  std::vector<TcArgs> probs(n);
+  // larger problems first, so the short ones fill the tail of the launch
+  std::vector<int> order(n);
+  std::vector<double> cost(n);
+  for (int i = 0; i < n; i++) {
+    const TcWorkspace &ws = *wss[i];
+    if (!ws.ready) fail(1, "tensor-core group: problem %d has no prepared batch", i);
+    if (ws.precision != P.precision) fail(1, "tensor-core group: mixed precisions");
+    const int nt = ws.Mp / BM;
+    cost[i] = (double)nt * (nt + 1) / 2 * ws.nen * ((double)ws.Kp / BK);
+    order[i] = i;
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<int4> work;
+  for (int oi = 0; oi < n; oi++) {
+    const int i = order[oi];
+    const TcWorkspace &ws = *wss[i];
+    TcArgs &a = probs[i];
+    const int nt = ws.Mp / BM, nkb = ws.Kp / BK;
+    const int ksub = ksub_of(ws);
+    a.Yt = ws.Yt; a.sB = ws.sB; a.sA = ws.sA; a.wt = ws.wt; a.Bp = ws.Bp;
+    a.Macc = (float2 *)ws.part;
+    a.slice = slice_of(ws.Mp, ws.nen);
+    a.Mp = ws.Mp; a.Kp = ws.Kp; a.nen = ws.nen; a.ntile_side = nt; a.ksub_blocks = ksub;
+    a.kb_split = kb_split_of(nkb, std::min(ws.nsplit, ws.nslice), ksub);
+    const int nsp = (nkb + a.kb_split - 1) / a.kb_split;
+    if (nsp > ws.nslice) fail(1, "tensor-core group: %d K splits for %d slices", nsp, ws.nslice);
+    for (int ta = 0; ta < nt; ta++)
+      for (int tb = ta; tb < nt; tb++)
+        for (int sp = 0; sp < nsp; sp++)
+          for (int c = 0; c < 2 * ws.nen; c++) work.push_back(make_int4(i, ta | (tb << 16), c, sp));
+  }
+  if (work.size() > 0x7fffffffu) fail(1, "tensor-core group: too many work items");
+  const size_t pbytes = ((sizeof(TcArgs) * n + 255) / 256) * 256, wbytes = sizeof(int4) * work.size();
+  grow(dev, have, pbytes + wbytes);
+  RP_CUDA(cudaMemcpyAsync(dev, probs.data(), sizeof(TcArgs) * n, cudaMemcpyHostToDevice, st));
+  RP_CUDA(cudaMemcpyAsync((unsigned char *)dev + pbytes, work.data(), wbytes, cudaMemcpyHostToDevice, st));
+  note_transfer((long long)(sizeof(TcArgs) * n + wbytes), 0);
+  P.probs = (const TcArgs *)dev;
+  P.work = (const int4 *)((unsigned char *)dev + pbytes);
+  P.nwork = (int)work.size();
+  P.smem = smem_of(P.precision);
+  if (P.smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", P.smem);
+  return P;
+}
+
+void (*kernel_of(int precision))(TcGroup) {
+  if (precision == RP_PREC_FP16X3) return tc_gram_kernel<3, true, false>;
+  if (precision == RP_PREC_BF16X3) return tc_gram_kernel<3, true, true>;
+  return tc_gram_kernel<2, false, false>;
+}
+
+int launch_group(const GroupPlan &P, int *err, cudaStream_t st) {
+  if (P.nwork == 0) return 0;
+  void (*kern)(TcGroup) = kernel_of(P.precision);
+  TcGroup g{P.probs, P.work, err};
+  kern<<<(unsigned)P.nwork, NTHREADS, P.smem, st>>>(g);
+  RP_CUDA(cudaGetLastError());
+  return 1;
+}
+
+void set_kernel_smem(int precision) {
+  static thread_local int done[4] = {0, 0, 0, 0};
+  const int idx = precision & 3;
+  if (done[idx]) return;
+  RP_CUDA(cudaFuncSetAttribute(kernel_of(precision), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem_of(precision)));
+  done[idx] = 1;
+}
+
+// times every distinct split of the prepared batch, keeps the fastest
+void tune_split(TcWorkspace &ws, int *err, cudaStream_t st) {
+  const int nkb = ws.Kp / BK, ksub = ksub_of(ws);
+  std::vector<int> cands;
+  int last_nsp = 0;
+  for (int s = 1; s <= SPLIT_MAX; s *= 2) {
+    const int kbs = kb_split_of(nkb, s, ksub), nsp = (nkb + kbs - 1) / kbs;
+    if (nsp != last_nsp && nsp <= ws.nslice) cands.push_back(s);
+    last_nsp = nsp;
+  }
+  TcWorkspace *one = &ws;
+  int best = 1;
+  float best_ms = 1e30f;
+  for (int rep = 0; rep < 2; rep++)  // the first pass warms up
+    for (int s : cands) {
+      ws.nsplit = s;
+      GroupPlan P = plan_group(&one, 1, st, g_scratch.dev, g_scratch.bytes);
+      RP_CUDA(cudaEventRecord(ws.ev0, st));
+      launch_group(P, err, st);
+      RP_CUDA(cudaEventRecord(ws.ev1, st));
+      RP_CUDA(cudaEventSynchronize(ws.ev1));
+      float ms = 0;
+      RP_CUDA(cudaEventElapsedTime(&ms, ws.ev0, ws.ev1));
+      if (rep == 1 && ms < best_ms) { best_ms = ms; best = s; }
+    }
+  ws.nsplit = best;
+  ws.tune_pending = 0;
+  // the candidates' sums are discarded
+  RP_CUDA(cudaMemsetAsync(ws.part, 0, sizeof(float2) * slice_of(ws.Mp, ws.nen) * ws.nslice, st));
+}
+}  // namespace
+
+int tc_prepare(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const double2 *w, const double2 *head,
+               int npair, int ntk, int ng, int nen, int g0, int precision, double2 *rowcol, int *err,
+               cudaStream_t st) {
+  ws.ready = 0;
   if (npair == 0) return 0;
+  if (ng != ws.ng || nen != ws.nen) fail(1, "tc_prepare: workspace begun for another q");
   int launches = 0;
   const int Gp = Gp_of(ng), Mp = 2 * Gp;
   const long Kn = (long)npair * ntk;
   const int Kp = (int)(((Kn + BK - 1) / BK) * BK);
-  const int nplanes = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2;
+  const int nplanes = nplanes_of(precision);
   // workspace: Yt [Mp][Kp] float, wt [nen][Kp] float4, maxes, scales, B planes
   const size_t ybytes = sizeof(float) * (size_t)Mp * Kp, wbytes = sizeof(float2) * 2 * (size_t)nen * Kp;
   const size_t mxbytes = sizeof(float) * (1 + 2 * (size_t)nen);
@@ -767,7 +1003,7 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
   wt_kernel<<<(unsigned)((Kn + 255) / 256), 256, 0, st>>>(w, npair, ntk, nen, Kp, wt);
   maxes_kernel<<<1024, 256, 0, st>>>(Yt, (size_t)Mp * Kp, wt, nen, Kp, Kn, maxes);
   rowmax_kernel<<<Mp, 256, 0, st>>>(Yt, Kp, Kn, rowmax);
-  const int exact = (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 1 : 0;
+  const int exact = nplanes == 3 ? 1 : 0;
   scales_kernel<<<(Mp + 127) / 128, 128, 0, st>>>(rowmax, maxes, Mp, nen, exact ? 7 : 14, sBv, sAv);
   launches += 5;
   RP_CUDA(cudaGetLastError());
@@ -777,18 +1013,8 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
     launches++;
     RP_CUDA(cudaGetLastError());
   }
-  // upper tiles of the symmetric Gram matrix
-  const int nt = Mp / BM;
-  std::vector<int2> tl;
-  for (int i = 0; i < nt; i++)
-    for (int j = i; j < nt; j++) tl.push_back(make_int2(i, j));
-  static thread_local void *d_tiles = nullptr;
-  static thread_local size_t d_tiles_bytes = 0;
-  grow(d_tiles, d_tiles_bytes, sizeof(int2) * tl.size());
-  RP_CUDA(cudaMemcpyAsync(d_tiles, tl.data(), sizeof(int2) * tl.size(), cudaMemcpyHostToDevice, st));
-  note_transfer((long long)(sizeof(int2) * tl.size()), 0);
   // B operand planes, shared by every (frequency, Re/Im) channel
-  const int nkb = Kp / BK;
+  const int nt = Mp / BM, nkb = Kp / BK;
   {
     dim3 g((unsigned)nkb, nt);
     if (precision == RP_PREC_FP16X3) bplanes_kernel<3, true, false><<<g, 256, 0, st>>>(Yt, sBv, Kp, nkb, Bp);
@@ -797,37 +1023,41 @@ int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, 
     launches++;
     RP_CUDA(cudaGetLastError());
   }
-  TcArgs a;
-  a.Yt = Yt; a.wt = wt; a.maxes = maxes; a.Macc = (float2 *)ws.part; a.err = err;
-  a.Mp = Mp; a.Kp = Kp; a.nen = nen; a.ntile_side = nt;
-  a.nplanes = nplanes;
-  a.bf16 = precision == RP_PREC_BF16X3 ? 1 : 0;
-  a.exact = exact;
-  a.sB = sBv; a.sA = sAv;
-  a.Bp = Bp;
-  // default 1024 K per FP32 sub-chunk: integer partial sums must stay below 2^24
-  a.ksub_blocks = ws.ksub > 0 ? ws.ksub : 16;
-  if (exact && a.ksub_blocks > 16) a.ksub_blocks = 16;
-  a.tiles = (const int2 *)d_tiles;
-  // per stage: A planes, B planes, the block's weights; then the barriers
-  const size_t smem = 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes * TILE_BYTES + 2 * (size_t)WBYTES + 256 +
-                      2 * sizeof(float) * BM;
-  if (smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", smem);
-  void (*kern)(TcArgs);
-  if (precision == RP_PREC_FP16X3) kern = tc_gram_kernel<3, true, false>;
-  else if (precision == RP_PREC_BF16X3) kern = tc_gram_kernel<3, true, true>;
-  else kern = tc_gram_kernel<2, false, false>;
-  RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid(2 * nen, (unsigned)tl.size());
+  ws.Yt = Yt; ws.sB = sBv; ws.sA = sAv; ws.wt = wt; ws.Bp = Bp;
+  ws.Mp = Mp; ws.precision = precision; ws.ready = 1;
+  set_kernel_smem(precision);
+  if (ws.tune_pending) {
+    const int kp_key = ws.Kp;  // the q's K estimate keys the cache
+    ws.Kp = Kp;
+    tune_split(ws, err, st);
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tuned[std::make_tuple(precision, Mp, nen, kbits(kp_key / BK))] = ws.nsplit;
+  }
+  ws.Kp = Kp;
+  return launches;
+}
+
+int tc_gram_group(TcWorkspace *const *wss, int n, int *err, cudaStream_t st) {
+  for (int i = 0; i < n; i++) set_kernel_smem(wss[i]->precision);
+  GroupPlan P = plan_group(wss, n, st, g_scratch.dev, g_scratch.bytes);
+  return launch_group(P, err, st);
+}
+
+int tc_contract_batch(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const double2 *w, const double2 *head,
+                      int npair, int ntk, int ng, int nen, int g0, int precision, double2 *chi, double2 *rowcol,
+                      int *err, cudaStream_t st) {
+  (void)chi;
+  if (npair == 0) return 0;
+  int launches = tc_prepare(ws, rho, rho64, w, head, npair, ntk, ng, nen, g0, precision, rowcol, err, st);
+  TcWorkspace *one = &ws;
   RP_CUDA(cudaEventRecord(ws.ev0, st));
-  kern<<<grid, NTHREADS, smem, st>>>(a);
+  launches += tc_gram_group(&one, 1, err, st);
   RP_CUDA(cudaEventRecord(ws.ev1, st));
-  launches++;
-  RP_CUDA(cudaGetLastError());
-  RP_CUDA(cudaStreamSynchronize(st));  // the workspace (and tile list) is reused by the next batch
+  RP_CUDA(cudaStreamSynchronize(st));  // the workspace (and work list) is reused by the next batch
   float ms = 0;
   RP_CUDA(cudaEventElapsedTime(&ms, ws.ev0, ws.ev1));
   ws.gram_seconds += ms * 1e-3;
+  ws.ready = 0;
   return launches;
 }
 
@@ -835,9 +1065,60 @@ int tc_end_q(TcWorkspace &ws, double2 *chi, double2 *rowcol, cudaStream_t st) {
   (void)rowcol;
   const int Gp = Gp_of(ws.ng), Mp = 2 * Gp;
   dim3 grid((unsigned)std::min<size_t>(((size_t)ws.ng * ws.ng + 255) / 256, 2048), ws.nen);
-  assemble_kernel<<<grid, 256, 0, st>>>((const float2 *)ws.part, Mp, Gp, ws.ng, ws.nen, chi);
+  assemble_kernel<<<grid, 256, 0, st>>>((const float2 *)ws.part, slice_of(Mp, ws.nen), ws.nslice, Mp, Gp, ws.ng,
+                                         chi);
   RP_CUDA(cudaGetLastError());
   return 1;
+}
+
+double tc_group_run(TcWorkspace *const *wss, int n, double2 *const *chis, int *err, cudaStream_t st, bool graph,
+                    long long *launches) {
+  if (n <= 0) return 0.0;
+  for (int i = 0; i < n; i++) set_kernel_smem(wss[i]->precision);
+  // the problem table and work list go up before any capture (host copies are not captured)
+  GroupPlan P = plan_group(wss, n, st, g_scratch.dev, g_scratch.bytes);
+  long long nl = 0;
+  auto enqueue = [&] {
+    nl += launch_group(P, err, st);
+    for (int i = 0; i < n; i++) nl += tc_end_q(*wss[i], chis[i], nullptr, st);
+  };
+  cudaEvent_t e0 = wss[0]->ev0, e1 = wss[0]->ev1;
+  if (graph) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    RP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue();
+    } catch (...) {
+      cudaStreamEndCapture(st, &g);  // leave the stream usable
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    RP_CUDA(cudaStreamEndCapture(st, &g));
+    const cudaError_t ie = cudaGraphInstantiate(&x, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      fail(-1, "CUDA graph of the ragged group: %s", cudaGetErrorString(ie));
+    }
+    RP_CUDA(cudaEventRecord(e0, st));
+    const cudaError_t le = cudaGraphLaunch(x, st);
+    RP_CUDA(cudaEventRecord(e1, st));
+    const cudaError_t se = cudaStreamSynchronize(st);
+    cudaGraphExecDestroy(x);
+    cudaGraphDestroy(g);
+    if (le != cudaSuccess) fail(-1, "CUDA graph launch: %s", cudaGetErrorString(le));
+    if (se != cudaSuccess) fail(-1, "ragged group: %s", cudaGetErrorString(se));
+  } else {
+    RP_CUDA(cudaEventRecord(e0, st));
+    enqueue();
+    RP_CUDA(cudaEventRecord(e1, st));
+    RP_CUDA(cudaStreamSynchronize(st));
+  }
+  float ms = 0;
+  RP_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  for (int i = 0; i < n; i++) wss[i]->ready = 0;
+  if (launches) *launches += nl;
+  return ms * 1e-3;
 }
 
 }  // namespace rp
