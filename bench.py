@@ -339,6 +339,136 @@ def run_gpu(args):
             dist.destroy_process_group()
 
 
+# --- ragged batch: many cells' chi0 problems in one tensor-core launch ---------
+
+RAGGED_CELLS = 12
+
+
+def ragged_specs(seed=7, ncell=RAGGED_CELLS):
+    """Seeded cells of the ragged workload: fcc/bcc/sc with a in [8, 14] bohr,
+    k meshes 3^3..6^3, 60-300 bands (8 occupied), wave-function cutoff 12-24 Ry
+    (raised where the sphere would hold fewer than 1.3x the bands, or to 1.5x
+    the dielectric cutoff), a target dielectric sphere of 40-400 G reached by
+    the dielectric cutoff, and 4-16 frequencies (half real 0-30 eV, half
+    imaginary)."""
+    from respackdev_gb300 import synth
+    rng = np.random.default_rng(seed)
+    vol_of = {"fcc": 0.25, "bcc": 0.5, "sc": 1.0}
+    cells = []
+    for i in range(ncell):
+        lat = ("fcc", "bcc", "sc")[i % 3]
+        a = float(rng.uniform(8.0, 14.0))
+        nk = int(rng.integers(3, 7))
+        nb = int(rng.integers(60, 301))
+        ecut = float(rng.uniform(12.0, 24.0))
+        vol = vol_of[lat] * a ** 3
+        npw = lambda e: vol * e ** 1.5 / (6 * np.pi ** 2)
+        while npw(ecut) < 1.3 * nb:
+            ecut *= 1.1
+        ng = int(rng.integers(40, 401))
+        ecut_eps = (6 * np.pi ** 2 * ng / vol) ** (2.0 / 3.0)
+        ecut = max(ecut, 1.5 * ecut_eps)  # the dielectric sphere stays well inside the density's
+        nen = int(rng.integers(4, 17))
+        nre = (nen + 1) // 2
+        em = np.concatenate([np.linspace(0.0, 30.0, nre),
+                             1j * np.linspace(30.0 / max(1, nen - nre), 30.0, nen - nre)]) / AU
+        spec = synth.SynthSpec(lattice=lat, a=a, nk=(nk, nk, nk), nbands=nb, nocc=8, ecut_psi=ecut,
+                               seed=1000 + i, wan_lo=9, wan_hi=11, shuffle_g=False)
+        cells.append((spec, ecut_eps, em))
+    return cells
+
+
+def _make_cell(args):
+    root, spec = args
+    from respackdev_gb300 import synth
+    synth.make_case(root, spec)
+    return root
+
+
+def run_ragged(args):
+    """One step = chi0 of every problem of the ragged workload (two q points of
+    each of the 12 cells) through rp_chi0_batch: preparation per problem, one
+    grouped tensor-core launch and the assembly in one CUDA graph.  The same
+    problems through rp_chi0_q one by one are timed beside it."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    tmp = tempfile.mkdtemp(prefix="rp_ragged_")
+    try:
+        cells = ragged_specs()
+        roots = [os.path.join(tmp, f"cell{i:02d}") for i in range(len(cells))]
+        for r in roots:
+            os.makedirs(r)
+        t0 = time.time()
+        # generate the cells in spawned processes before any GPU call, one BLAS
+        # thread each (the workers inherit the environment at spawn)
+        blas = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
+        saved = {k: os.environ.get(k) for k in blas}
+        os.environ.update({k: "1" for k in blas})
+        try:
+            with cf.ProcessPoolExecutor(max_workers=min(8, os.cpu_count() or 1),
+                                        mp_context=mp.get_context("spawn")) as ex:
+                list(ex.map(_make_cell, [(r, c[0]) for r, c in zip(roots, cells)]))
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        gen = time.time() - t0
+        from respackdev_gb300 import chiqw as rp
+        rp.load()
+        ctxs = []
+        for r, (spec, ecut_eps, em) in zip(roots, cells):
+            p = rp.default_params(precision=rp.PREC_FP16X3, ecut_for_eps=ecut_eps, green_func_delt=0.2721, flg_crpa=1)
+            ctxs.append(rp.Context(r, p, em))
+        probs, shapes = [], []
+        for i, (c, (spec, _, em)) in enumerate(zip(ctxs, cells)):
+            nq = c.L.rp_num_qirr(c._h)
+            qs = [1, nq // 2 + 1] if i % 3 == 0 else [2, nq // 2 + 1]
+            for iq in qs:
+                ng, nd = c.q_dims(iq)
+                inf = c.info()
+                probs.append((c, iq))
+                shapes.append({"cell": i, "lattice": spec.lattice, "a": round(spec.a, 3), "nk": spec.nk[0],
+                               "bands": spec.nbands, "npw_max": inf.ntg, "q": iq, "ng": ng, "ndir": nd,
+                               "nen": inf.nen, "npair": inf.n_occ * inf.n_vir})
+        for _ in range(max(1, args.warmup)):
+            rp.chi0_batch(probs, graph=True, fetch=False)
+        launches0 = sum(c.kernel_launches() for c in ctxs)
+        t0 = time.perf_counter()
+        secs = np.zeros(3)
+        for _ in range(args.steps):
+            _, s = rp.chi0_batch(probs, graph=True, fetch=False)
+            secs += s
+        batch = (time.perf_counter() - t0) / args.steps
+        launches = (sum(c.kernel_launches() for c in ctxs) - launches0) // args.steps
+        t0 = time.perf_counter()
+        seq_gram = 0.0
+        for _ in range(args.steps):
+            for c, iq in probs:
+                c.chi0_q(iq, fetch=False)
+                seq_gram += c.tc_gram_seconds()
+        seq = (time.perf_counter() - t0) / args.steps
+        seq_gram /= args.steps
+        n = len(probs)
+        line = {"metric": "chiqw ragged batch s/problem (all w), 12 cells in one grouped launch",
+                "value": batch / n, "unit": "s/problem", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": False, "dtype": "fp16x3-split tensor contraction, f32 pair densities",
+                "data": "synthetic (seeded generator, 12 cells)",
+                "config": {"workload": "chiqw_ragged_12cells", "problems": n, "cells": len(cells)},
+                "sequential_s_per_problem": seq / n, "speedup_vs_sequential": seq / batch,
+                "sequential_gram_device_seconds": seq_gram,
+                "batch_seconds": {"prepare": secs[0] / args.steps, "graph_device": secs[1] / args.steps,
+                                  "finish": secs[2] / args.steps},
+                "gram_launches_per_batch": 1, "gpu_launches_per_batch": int(launches),
+                "tuned_shapes": rp.tuned_shapes(), "input_generation_seconds": gen, "shapes": shapes}
+        print(json.dumps(line), flush=True)
+        for c in ctxs:
+            c.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,11 +477,14 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
-    ap.add_argument("--case", default="full", choices=["full", "small"],
-                    help="small: 4x4x4 k, 100 bands, same kernels (for profiler captures)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "ragged"],
+                    help="small: 4x4x4 k, 100 bands, same kernels (for profiler captures); "
+                         "ragged: 12 cells' chi0 problems in one grouped launch")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.case == "ragged":
+        run_ragged(args)
     else:
         run_gpu(args)
 

@@ -15,9 +15,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "rp_dev.cuh"
@@ -675,26 +677,57 @@ int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, dou
     RP_CUDA(cudaSetDevice(c0->dev));
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
-    std::vector<std::unique_ptr<Prob>> P;
+    std::vector<std::unique_ptr<Prob>> P(n);
     for (int i = 0; i < n; i++) {
-      rp_ctx *c = ctxs[i];
-      auto p = std::make_unique<Prob>();
-      p->c = c;
-      c->have_chi = c->have_eps = false;
-      p->task = rp::make_qtask(c->S, iqs[i] - 1, c->S.params.max_pairs);
-      p->r.iq = iqs[i]; p->r.fast = true; p->r.t = &p->task; p->r.chi = &p->chi; p->r.rowcol = &p->rowcol;
-      q_begin(c, p->r);
-      for (int bi = 0; bi < q_nbatch(p->r); bi++) {
-        auto ws = std::make_unique<rp::TcWorkspace>();
-        ws->ksub = c->S.params.tc_ksub;
-        rp::tc_begin_q(*ws, p->r.ng, p->r.nen, p->r.ndir, c->S.params.tc_split,
-                       (long)q_batch_pairs(p->r, bi) * p->r.ntk, prec, c->st);
-        p->ws.push_back(std::move(ws));
-        q_batch(c, p->r, bi, p->ws.back().get(), false);
-      }
-      check_device_error(c);
-      P.push_back(std::move(p));
+      P[i] = std::make_unique<Prob>();
+      P[i]->c = ctxs[i];
     }
+    // preparation: the problems of one context in order on its stream (they
+    // share its pair-density buffers), the contexts concurrently, one host
+    // thread each, so small problems of different cells overlap on the GPU
+    std::vector<rp_ctx *> uniq;
+    for (int i = 0; i < n; i++)
+      if (std::find(uniq.begin(), uniq.end(), ctxs[i]) == uniq.end()) uniq.push_back(ctxs[i]);
+    std::vector<std::exception_ptr> errs(uniq.size());
+    std::vector<long long> h2d(uniq.size(), 0), d2h(uniq.size(), 0);
+    auto prepare = [&](size_t u) {
+      rp_ctx *c = uniq[u];
+      const long long h0 = t_h2d, d0 = t_d2h;
+      try {
+        RP_CUDA(cudaSetDevice(c->dev));
+        c->have_chi = c->have_eps = false;
+        for (int i = 0; i < n; i++) {
+          if (ctxs[i] != c) continue;
+          Prob &p = *P[i];
+          p.task = rp::make_qtask(c->S, iqs[i] - 1, c->S.params.max_pairs);
+          p.r.iq = iqs[i]; p.r.fast = true; p.r.t = &p.task; p.r.chi = &p.chi; p.r.rowcol = &p.rowcol;
+          q_begin(c, p.r);
+          for (int bi = 0; bi < q_nbatch(p.r); bi++) {
+            auto ws = std::make_unique<rp::TcWorkspace>();
+            ws->ksub = c->S.params.tc_ksub;
+            rp::tc_begin_q(*ws, p.r.ng, p.r.nen, p.r.ndir, c->S.params.tc_split,
+                           (long)q_batch_pairs(p.r, bi) * p.r.ntk, prec, c->st);
+            p.ws.push_back(std::move(ws));
+            q_batch(c, p.r, bi, p.ws.back().get(), false);
+          }
+          check_device_error(c);
+        }
+      } catch (...) {
+        errs[u] = std::current_exception();
+      }
+      h2d[u] = t_h2d - h0;
+      d2h[u] = t_d2h - d0;
+    };
+    {
+      std::vector<std::thread> th;
+      for (size_t u = 1; u < uniq.size(); u++) th.emplace_back(prepare, u);
+      prepare(0);
+      for (auto &x : th) x.join();
+    }
+    for (size_t u = 1; u < uniq.size(); u++) { t_h2d += h2d[u]; t_d2h += d2h[u]; }
+    for (auto &e : errs)
+      if (e) std::rethrow_exception(e);
+    RP_CUDA(cudaSetDevice(c0->dev));
     const auto t1 = clk::now();
     // one grouped Gram launch over every prepared batch, then each batch into its problem's chi
     std::vector<rp::TcWorkspace *> wl;

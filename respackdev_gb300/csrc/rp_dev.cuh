@@ -45,6 +45,29 @@ __device__ inline void cfma(float2 &a, float2 b, float2 c) {
     if (_e != cudaSuccess) ::rp::fail(-1, "%s: %s (%s:%d)", #call, cudaGetErrorString(_e), __FILE__, __LINE__); \
   } while (0)
 
+// Opt-in shared memory per block of the current device.  Kernels with large
+// tiles get this as their cap once and for all (the launch's own size decides
+// occupancy), so launches from several host threads never see a smaller cap
+// that another thread set for its own launch.
+inline int smem_optin_bytes() {
+  static int v = 0;
+  if (!v) {
+    int d = 0, x = 0;
+    if (cudaGetDevice(&d) != cudaSuccess ||
+        cudaDeviceGetAttribute(&x, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) != cudaSuccess)
+      return 48 * 1024;  // the launch that follows reports the error
+    v = x;
+  }
+  return v;
+}
+// the largest dynamic shared memory a kernel may be given: the opt-in total
+// less the kernel's static shared memory
+template <typename K> inline int smem_cap(K kern) {
+  cudaFuncAttributes fa;
+  if (cudaFuncGetAttributes(&fa, (const void *)kern) != cudaSuccess) return 48 * 1024;
+  return smem_optin_bytes() - (int)fa.sharedSizeBytes;
+}
+
 // ---- launchers (each returns the number of kernels it launched) -------------
 
 // Full-k coefficients and real-space periodic parts (K1 + K2):

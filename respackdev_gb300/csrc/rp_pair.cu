@@ -501,7 +501,7 @@ int launch_pair_density_fp64(const float2 *ur, const PairGeom &g, const PairChun
   if (g.n1 > 1023 || g.n2 > 1023 || g.n3 > 1023) fail(1, "FFT box dimension above 1023");
   const size_t smem = pair_density_smem(g, c.jmax, true);
   if (smem > 227 * 1024) fail(1, "pair-density tile needs %zu bytes of shared memory", smem);
-  RP_CUDA(cudaFuncSetAttribute(pair_density_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RP_CUDA(cudaFuncSetAttribute(pair_density_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(pair_density_kernel<double>)));
   dim3 grid(g.ntk, c.nchunk);
   pair_density_kernel<double><<<grid, 256, smem, st>>>(ur, pair_args(g, c), out);
   RP_CUDA(cudaGetLastError());
@@ -526,7 +526,7 @@ int launch_pair_density_fp32(const float2 *ur, const PairGeom &g, const PairChun
     case 14: kern = split ? pair_slab_kernel<14, true> : pair_slab_kernel<14, false>; break;
     default: break;
   }
-  RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(kern)));
   dim3 grid(c.nchunk, g.ntk);
   kern<<<grid, PD_THREADS, smem, st>>>(ur, pair_args(g, c), out);
   RP_CUDA(cudaGetLastError());

@@ -855,6 +855,9 @@ namespace {
 struct GroupScratch {
   void *dev = nullptr;
   size_t bytes = 0;
+  ~GroupScratch() {
+    if (dev) cudaFree(dev);
+  }
 };
 thread_local GroupScratch g_scratch;
 
@@ -936,7 +939,7 @@ void set_kernel_smem(int precision) {
   const int idx = precision & 3;
   if (done[idx]) return;
   RP_CUDA(cudaFuncSetAttribute(kernel_of(precision), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)smem_of(precision)));
+                               smem_cap(kernel_of(precision))));
   done[idx] = 1;
 }
 

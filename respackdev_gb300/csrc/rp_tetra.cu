@@ -775,7 +775,7 @@ int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st) {
   while (nec > 1 && (size_t)a.ntk * nec * 3 * sizeof(double2) > budget) nec--;
   size_t smem = (size_t)a.ntk * nec * 3 * sizeof(double2) + fixed;
   if (smem > 227 * 1024) fail(1, "k mesh too large for the tetrahedron tile (%zu bytes)", smem);
-  RP_CUDA(cudaFuncSetAttribute(tetra_weights_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RP_CUDA(cudaFuncSetAttribute(tetra_weights_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(tetra_weights_kernel)));
   dim3 grid(a.npair, (a.nen + nec - 1) / nec);
   tetra_weights_kernel<<<grid, 256, smem, st>>>(a, nec, w);
   RP_CUDA(cudaGetLastError());
@@ -848,7 +848,7 @@ int launch_intraband(const TetraArgs &a, const double2 *cfull, const int *ng0, c
   if (nb == 0) return 0;
   size_t smem = (size_t)a.ntk * (sizeof(double2) + 3 * sizeof(double) + sizeof(cx));
   if (smem > 227 * 1024) fail(1, "k mesh too large for the intraband tile");
-  RP_CUDA(cudaFuncSetAttribute(intraband_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RP_CUDA(cudaFuncSetAttribute(intraband_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(intraband_kernel)));
   intraband_kernel<<<nb, 256, smem, st>>>(a, cfull, ng0, kg0, ncb, ntg, bvec9, sk0, bands, pwpl);
   RP_CUDA(cudaGetLastError());
   return 1;

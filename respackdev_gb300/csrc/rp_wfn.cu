@@ -104,7 +104,7 @@ int launch_wfn_realspace(const double2 *coef_irr, const int *numirr, const int *
   size_t smem = sizeof(double2) * ((size_t)D1 * D2 * D3 + D1 * D2 + D1 * n2 + n1 + n2 + n3) +
                 sizeof(int) * (D1 + D2 + D3);
   if (smem > 200 * 1024) fail(1, "plane-wave sphere too large for the shared-memory cube (%zu bytes)", smem);
-  RP_CUDA(cudaFuncSetAttribute(wfn_realspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  RP_CUDA(cudaFuncSetAttribute(wfn_realspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(wfn_realspace_kernel)));
   dim3 grid(ncb, k_end - k_begin);
   wfn_realspace_kernel<<<grid, 256, smem, st>>>(coef_irr, numirr, trs, src, phase, ng0, kg0, ncb, ntg, n1, n2,
                                                 n3, R1, R2, R3, cfull, ur, k_begin);
