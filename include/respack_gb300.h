@@ -64,6 +64,9 @@ typedef struct rp_params {
                                   q (0 = as many as fit in 24 GB)             */
   int    tc_split;             /* K splits of the tensor-core Gram launch (0 =
                                   measured per shape by the split tuner)      */
+  int    write_eps_f32;        /* 1: rp_write_q also writes dat.epsqw.c4, the
+                                  complex(4) eps^-1 calc_int reads (Gamma: the
+                                  mean of the three directions)              */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */
@@ -199,6 +202,8 @@ typedef struct rp_int_params {
   int    fft_box[3];           /* 0 0 0: reference rule (calc_intW.F:150-185) */
   int    device;
   int    write_files;          /* 1: write dir-intW / dir-intJ / dir-mvmc */
+  int    read_eps_f32;         /* 1: read dir-eps/qNNN/dat.epsqw.c4 where it
+                                  exists instead of dat.epsqw.600(-602)       */
 } rp_int_params;
 
 void rp_int_default_params(rp_int_params *p);

@@ -15,7 +15,8 @@ class IntParams(C.Structure):
     _fields_ = [("calc_ifreq", C.c_int), ("ix_intj_min", C.c_int), ("ix_intj_max", C.c_int),
                 ("iy_intj_min", C.c_int), ("iy_intj_max", C.c_int), ("iz_intj_min", C.c_int),
                 ("iz_intj_max", C.c_int), ("wcut_mvmc", C.c_double), ("jcut_mvmc", C.c_double),
-                ("fft_box", C.c_int * 3), ("device", C.c_int), ("write_files", C.c_int)]
+                ("fft_box", C.c_int * 3), ("device", C.c_int), ("write_files", C.c_int),
+                ("read_eps_f32", C.c_int)]
 
 
 _bound = False

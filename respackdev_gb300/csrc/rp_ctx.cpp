@@ -597,6 +597,21 @@ static void write_q(rp_ctx *c, const std::string &root) {
     snprintf(buf, sizeof buf, "/dat.epsqw.%03d", S.params.file_num_eps_start + ix);
     rp::write_unformatted_record(qdir + buf, &c->h_eps[ix * m], sizeof(cd) * m);
   }
+  if (S.params.write_eps_f32) {
+    // what calc_int keeps of eps^-1 (epsirr, complex(4); calc_intW.F:587-630):
+    // at Gamma the mean of the three directions, summed and divided in the
+    // order its reader uses, so reading this file gives the same values at
+    // half the bytes of one FP64 record
+    std::vector<float> c4(2 * m);
+    for (size_t i = 0; i < m; i++) {
+      cd acc(0.0, 0.0);
+      for (int ix = 0; ix < c->ndir; ix++) acc += c->h_eps[ix * m + i];
+      if (c->ndir == 3) acc = acc / 3.0;
+      c4[2 * i] = (float)acc.real();
+      c4[2 * i + 1] = (float)acc.imag();
+    }
+    rp::write_unformatted_record(qdir + "/dat.epsqw.c4", c4.data(), sizeof(float) * c4.size());
+  }
   // the completion flag is written last, so an interrupted run resumes at this q
   snprintf(buf, sizeof buf, "/dat.log.%03d", S.params.file_num_log_start);
   FILE *f = fopen((qdir + buf).c_str(), "w");

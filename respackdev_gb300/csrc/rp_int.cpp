@@ -316,21 +316,36 @@ static void int_read_eps_dir(rp_int *c) {
     const bool gm = std::fabs(k[0]) < 1e-5 && std::fabs(k[1]) < 1e-5 && std::fabs(k[2]) < 1e-5;
     const int NG = c->nge[iq], nf = gm ? 3 : 1;
     if (gm) c->iqgm = iq;
-    std::vector<cd> acc((size_t)NG * NG * c->ne, cd(0, 0)), buf(acc.size());
-    for (int ix = 0; ix < nf; ix++) {
-      rp::UnformattedReader r(d + fmt("q%03d/dat.epsqw.%03d", iq + 1, 600 + ix));
-      const size_t got = r.read(buf.data(), sizeof(cd) * buf.size());
-      if (got != sizeof(cd) * buf.size()) fail(1, "dir-eps/q%03d/dat.epsqw.%03d: %zu bytes, expected %zu", iq + 1, 600 + ix, got, sizeof(cd) * buf.size());
-      for (size_t i = 0; i < acc.size(); i++) acc[i] += buf[i];
-    }
     std::fill(host.begin(), host.end(), make_float2(0.f, 0.f));
-    for (int e = 0; e < c->ne; e++)
-      for (int jg = 0; jg < NG; jg++)
-        for (int ig = 0; ig < NG; ig++) {
-          cd v = acc[((size_t)e * NG + jg) * NG + ig];
-          if (gm) v = v / 3.0;
-          host[((size_t)e * c->ntgq + jg) * c->ntgq + ig] = make_float2((float)v.real(), (float)v.imag());
-        }
+    const std::string c4path = d + fmt("q%03d/dat.epsqw.c4", iq + 1);
+    struct stat st4;
+    if (c->P.read_eps_f32 && stat(c4path.c_str(), &st4) == 0) {
+      // the complex(4) side file of rp_write_q (write_eps_f32): the values below, precomputed
+      std::vector<float2> b4((size_t)NG * NG * c->ne);
+      rp::UnformattedReader r(c4path);
+      const size_t got = r.read(b4.data(), sizeof(float2) * b4.size());
+      if (got != sizeof(float2) * b4.size())
+        fail(1, "dir-eps/q%03d/dat.epsqw.c4: %zu bytes, expected %zu", iq + 1, got, sizeof(float2) * b4.size());
+      for (int e = 0; e < c->ne; e++)
+        for (int jg = 0; jg < NG; jg++)
+          for (int ig = 0; ig < NG; ig++)
+            host[((size_t)e * c->ntgq + jg) * c->ntgq + ig] = b4[((size_t)e * NG + jg) * NG + ig];
+    } else {
+      std::vector<cd> acc((size_t)NG * NG * c->ne, cd(0, 0)), buf(acc.size());
+      for (int ix = 0; ix < nf; ix++) {
+        rp::UnformattedReader r(d + fmt("q%03d/dat.epsqw.%03d", iq + 1, 600 + ix));
+        const size_t got = r.read(buf.data(), sizeof(cd) * buf.size());
+        if (got != sizeof(cd) * buf.size()) fail(1, "dir-eps/q%03d/dat.epsqw.%03d: %zu bytes, expected %zu", iq + 1, 600 + ix, got, sizeof(cd) * buf.size());
+        for (size_t i = 0; i < acc.size(); i++) acc[i] += buf[i];
+      }
+      for (int e = 0; e < c->ne; e++)
+        for (int jg = 0; jg < NG; jg++)
+          for (int ig = 0; ig < NG; ig++) {
+            cd v = acc[((size_t)e * NG + jg) * NG + ig];
+            if (gm) v = v / 3.0;
+            host[((size_t)e * c->ntgq + jg) * c->ntgq + ig] = make_float2((float)v.real(), (float)v.imag());
+          }
+    }
     RP_CUDA(cudaMemcpyAsync(c->eps.as<float2>() + (size_t)iq * nn * c->ne, host.data(), sizeof(float2) * host.size(),
                             cudaMemcpyHostToDevice, c->st));
     RP_CUDA(cudaStreamSynchronize(c->st));
@@ -873,6 +888,7 @@ void rp_int_default_params(rp_int_params *p) {
   p->wcut_mvmc = 2.0;
   p->jcut_mvmc = 0.3;
   p->write_files = 1;
+  p->read_eps_f32 = 1;
 }
 
 int rp_int_parse_namelist(const char *text, rp_int_params *p) {

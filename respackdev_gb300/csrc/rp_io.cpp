@@ -288,6 +288,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "tc_ksub") p->tc_ksub = nl_int(v, k);
       else if (k == "pair_batch") p->pair_batch = nl_int(v, k);
       else if (k == "tc_split") p->tc_split = nl_int(v, k);
+      else if (k == "write_eps_f32") p->write_eps_f32 = nl_int(v, k);
       else if (k == "freq_re_ev") for (auto &x : v) fre.push_back(to_num(x));
       else if (k == "freq_im_ev") for (auto &x : v) fim.push_back(to_num(x));
       else fail(1, "namelist &param_gpu: unknown name '%s'", k.c_str());
@@ -354,6 +355,7 @@ void parse_calc_int_namelist(const std::string &text, rp_int_params *p) {
         for (int i = 0; i < 3; i++) p->fft_box[i] = (int)llround(to_num(v[i]));
       } else if (k == "device") p->device = nl_int(v, k);
       else if (k == "write_files") p->write_files = nl_int(v, k);
+      else if (k == "read_eps_f32") p->read_eps_f32 = nl_int(v, k);
       else fail(1, "namelist &param_gpu: unknown name '%s' for calc_int", k.c_str());
     }
   }

@@ -108,8 +108,9 @@ def test_files_match_arrays(int_case, int_copy):
 
 def test_calc_int_namelist_parser():
     p = ci.parse_namelist("&param_calc_int\n CALC_IFREQ=3, IX_INTJ_MIN=-1, ix_intJ_max=2\n"
-                          " wcut_mvmc=1.5 /\n&param_gpu\n fft_box=8 8 8 /\n")
+                          " wcut_mvmc=1.5 /\n&param_gpu\n fft_box=8 8 8, read_eps_f32=0 /\n")
     assert (p.calc_ifreq, p.ix_intj_min, p.ix_intj_max, p.iy_intj_min) == (3, -1, 2, 0)
+    assert p.read_eps_f32 == 0 and ci.default_params().read_eps_f32 == 1
     assert p.wcut_mvmc == 1.5 and p.jcut_mvmc == 0.3 and list(p.fft_box) == [8, 8, 8]
     with pytest.raises(ValueError):
         ci.parse_namelist("&param_calc_int\n bogus=1 /\n")

@@ -73,3 +73,34 @@ def test_bad_range_is_an_input_error(int_case, int_copy):
     with ci.IntContext(root, p) as c:
         with pytest.raises(RuntimeError, match="intJ range"):
             c.j3d()
+
+
+def test_complex4_eps_side_file_gives_the_same_w(int_case, int_copy):
+    """dir-eps written by rp_calc_chiqw with write_eps_f32=1 carries
+    dat.epsqw.c4 beside the FP64 records: complex(4) eps^-1 (Gamma: the mean
+    of the three directions), what calc_int keeps of eps^-1 anyway.  W and J
+    from the side files equal W and J from the FP64 records exactly, and the
+    side file is half an FP64 record."""
+    import shutil
+    from respackdev_gb300 import chiqw as rp
+    from tests.helpers import EM_INT, namelist_text
+    root = int_copy(int_case("tiny_wan"))
+    shutil.rmtree(os.path.join(root, "dir-eps"))
+    rp.calc_chiqw(root, namelist_text(dict(green_func_delt=0.2721, ecut_for_eps=3.0), EM_INT,
+                                      "precision='fp64', write_eps_f32=1"))
+    qdirs = sorted(d for d in os.listdir(os.path.join(root, "dir-eps")) if d.startswith("q"))
+    assert qdirs
+    for q in qdirs:
+        c4 = os.path.getsize(os.path.join(root, "dir-eps", q, "dat.epsqw.c4"))
+        f8 = os.path.getsize(os.path.join(root, "dir-eps", q, "dat.epsqw.600"))
+        assert c4 - 8 == (f8 - 8) // 2, (q, c4, f8)   # payload halves (4-byte record markers)
+    out = {}
+    for use in (0, 1):
+        p = ci.default_params(ix_intj_min=0, ix_intj_max=1, write_files=0, read_eps_f32=use)
+        with ci.IntContext(root, p) as c:
+            out[use] = (c.w3d(), c.j3d())
+    (V0, W0), (X0, J0) = out[0]
+    (V1, W1), (X1, J1) = out[1]
+    assert np.array_equal(V0, V1) and np.array_equal(X0, X1)
+    assert np.array_equal(W0, W1) and np.array_equal(J0, J1)
+
