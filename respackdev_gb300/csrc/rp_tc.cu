@@ -25,7 +25,12 @@
 // global memory (tile-blocked, rows contiguous, so a warp's 32 rows are one
 // coalesced access), converted to FP64 once when chi is assembled.
 //
-// Kernel layout: one CTA per (upper tile, frequency, Re/Im weight), 704 threads.
+// Kernel layout: one CTA of 704 threads per work item -- (problem, upper tile,
+// frequency, Re/Im weight, K split) -- of a work list.  A q point is a group of
+// one problem; a ragged batch (several q points of several cells) is one
+// launch over all its problems.  Small problems split K across CTAs, each
+// split into its own slice of the sums, added when chi is assembled; the split
+// of a shape is measured once and cached (tc_begin_q, tune_split).
 //   warps 0-15  producers (8 rows each): read the FP32 rows of the A operand (prefetched one K
 //               block ahead in registers), multiply by the weights, split into
 //               planes and store them into shared memory in the 128-byte-swizzled
