@@ -79,8 +79,9 @@ struct rp_ctx {
   bool have_chi = false, have_eps = false;
   bool eps_fallback = false;  // the last rp_epsinv_q fell back to the FP64 inversion
   std::vector<cd> h_chi, h_eps;
-  void *stage = nullptr;       // pinned two-slot staging buffer of device->host copies
-  cudaEvent_t sev[2]{};        // completion of each slot's copy
+  static constexpr int NSLOT = 4;  // pinned staging slots of device->host copies (one per host thread)
+  void *stage = nullptr;           // NSLOT slots of 8 MB
+  cudaEvent_t sev[NSLOT]{};        // completion of each slot's copy
   cudaEvent_t ev[6]{};
   double times[6]{};
   long long h2d = 0, d2h = 0;  // bytes moved between host and device by this context's calls
@@ -514,30 +515,43 @@ static void epsinv_run(rp_ctx *c) {
   c->have_eps = true;
 }
 
-// Device -> host copy of `bytes` into any host memory: chunks go through two
-// pinned slots, so the host copy of chunk i out of its slot overlaps the
-// device copy of chunk i+1 into the other, and pageable destinations move at
-// pinned-copy speed.
+// Device -> host copy of `bytes` into any host memory.  Chunks go through
+// pinned slots, one per host thread: thread t copies chunks t, t + T, ... --
+// device copy into its slot, then the host copy out of it -- so the host
+// copies (and the first touch of fresh pageable pages) run in parallel and
+// overlap the device copies of the other threads' chunks.
 static void fetch_to(rp_ctx *c, const void *src, void *dst, size_t bytes) {
   constexpr size_t CH = (size_t)8 << 20;
   if (!c->stage) {
-    RP_CUDA(cudaMallocHost(&c->stage, 2 * CH));
+    RP_CUDA(cudaMallocHost(&c->stage, rp_ctx::NSLOT * CH));
     for (auto &e : c->sev) RP_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
   const size_t n = (bytes + CH - 1) / CH;
-  auto issue = [&](size_t i) {
-    const size_t o = i * CH, len = std::min(CH, bytes - o);
-    RP_CUDA(cudaMemcpyAsync((char *)c->stage + (i & 1) * CH, (const char *)src + o, len, cudaMemcpyDeviceToHost,
-                            c->st));
-    RP_CUDA(cudaEventRecord(c->sev[i & 1], c->st));
+  const int T = (int)std::min<size_t>(rp_ctx::NSLOT, n);
+  std::exception_ptr errs[rp_ctx::NSLOT];
+  auto worker = [&](int t) {
+    try {
+      RP_CUDA(cudaSetDevice(c->dev));
+      char *slot = (char *)c->stage + (size_t)t * CH;
+      for (size_t j = (size_t)t; j < n; j += (size_t)T) {
+        const size_t o = j * CH, len = std::min(CH, bytes - o);
+        RP_CUDA(cudaMemcpyAsync(slot, (const char *)src + o, len, cudaMemcpyDeviceToHost, c->st));
+        RP_CUDA(cudaEventRecord(c->sev[t], c->st));
+        RP_CUDA(cudaEventSynchronize(c->sev[t]));
+        std::memcpy((char *)dst + o, slot, len);
+      }
+    } catch (...) {
+      errs[t] = std::current_exception();
+    }
   };
-  for (size_t i = 0; i < n && i < 2; i++) issue(i);
-  for (size_t i = 0; i < n; i++) {
-    RP_CUDA(cudaEventSynchronize(c->sev[i & 1]));
-    const size_t o = i * CH;
-    std::memcpy((char *)dst + o, (const char *)c->stage + (i & 1) * CH, std::min(CH, bytes - o));
-    if (i + 2 < n) issue(i + 2);
+  {
+    std::vector<std::thread> th;
+    for (int t = 1; t < T; t++) th.emplace_back(worker, t);
+    if (T > 0) worker(0);
+    for (auto &x : th) x.join();
   }
+  for (int t = 0; t < T; t++)
+    if (errs[t]) std::rethrow_exception(errs[t]);
   t_d2h += (long long)bytes;
 }
 
