@@ -41,6 +41,7 @@ sys.path.insert(0, HERE)
 
 AU = 27.21151
 WORKLOAD = "chiqw_8x8x8k_200b"
+METRIC = "chiqw s/q-point (all w) vs plain FP64 GPU at chi rel err<=1e-6; % roofline"
 
 
 def make_spec(case="full"):
@@ -179,11 +180,12 @@ def run_reference(args):
             vals.append(v)
         wall = time.time() - t0
         value = float(np.mean(vals))
-        line = {"metric": "chiqw s/q-point (all w)", "value": value, "unit": "s/q-point", "impl": "reference",
+        line = {"metric": METRIC, "value": value, "unit": "s/q-point", "impl": "reference",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
                 "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "npair": rep.npair_full_last, "ng": rep.ng_last, "ntk": rep.ntk,
-                           "nen": rep.nen, "fft_box": list(rep.fft_box), "parallelism": "openmp-host"},
+                "config": {"workload": WORKLOAD, "ntk": rep.ntk, "nbands": make_spec().nbands,
+                           "npair": rep.npair_full_last, "ng": rep.ng_last, "nen": rep.nen,
+                           "fft_box": list(rep.fft_box), "parallelism": "openmp-host"},
                 "cpu_baseline": {"value": value, "unit": "s/q-point", "cores": nthreads, "kind": "port",
                                  "sample": f"one q point, {rep.npair_last} of {rep.npair_full_last} band pairs, "
                                            f"scaled linearly in the pair count (C restatement of chiqw; the Fortran "
@@ -312,7 +314,7 @@ def run_gpu(args):
                              f"scaled linearly in the pair count"}
         clocks = clk.summary()
         if rank == 0:
-            line = {"metric": "chiqw s/q-point (all w) vs plain FP64 GPU at chi rel err<=1e-6; % roofline",
+            line = {"metric": METRIC,
                     "value": value, "unit": "s/q-point", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                     "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": False, "scaling": "weak",
                     "vs_baseline": None, "dtype": "fp16x3-split tensor contraction, f32 pair densities, f64 weights/eps",
