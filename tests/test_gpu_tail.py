@@ -62,7 +62,7 @@ def test_training_fits_a_smooth_map():
 # --- band-tail correction on synthetic cells ---------------------------------
 
 EM = np.array([0.0, 2.0, 6.0, 0.5j, 3.0j]) / synth.AU_EV
-NTRUNC, NFULL, NSHELL = 12, 36, 4
+NTRUNC, NFULL, NSHELL = 12, 36, 8
 QS = list(range(2, 9))        # the q != 0 points of the 2x2x2 mesh
 
 
