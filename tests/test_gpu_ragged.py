@@ -76,10 +76,10 @@ def test_ragged_batch_matches_single_q(cells, prec):
 
 
 def test_ragged_batch_against_oracle(cells, tmp_path):
-    """Problems of two cells from one batch against the FP64 oracle (1e-6)."""
+    """Problems of all three cells from one batch against the FP64 oracle (1e-6)."""
     import shutil
     roots = {}
-    for name in ("fcc", "sc"):
+    for name in ("fcc", "bcc", "sc"):
         d, ecut, em = cells[name]
         r = os.path.join(str(tmp_path), name)
         for sub in ("dir-wfn", "dir-wan"):
