@@ -158,6 +158,31 @@ def test_chi0_matches_planewave_bruteforce(case_dir, fresh_copy, qidx):
     assert err < 1e-6, err
 
 
+@pytest.mark.parametrize("lattice,a,nk,ecut_psi", [("bcc", 8.5, (2, 2, 2), 7.0), ("sc", 7.0, (2, 2, 2), 7.0)])
+def test_chi0_bruteforce_other_lattices(tmp_path, lattice, a, nk, ecut_psi):
+    """The same plane-wave check on a body-centred and a simple cubic cell,
+    with an alias-free box from the cell's own plane-wave extent."""
+    spec = synth.SynthSpec(lattice=lattice, a=a, nk=nk, nbands=10, nocc=4, ecut_psi=ecut_psi, seed=41,
+                           wan_lo=5, wan_hi=7)
+    root = str(tmp_path)
+    d = synth.make_case(root, spec)
+    ext = np.max([np.abs(g).max(0) for g in d.kg], axis=0)
+    box = tuple(int(4 * r + 2) for r in ext)
+    em = np.array([0.0, 0.2, 0.1 + 0.05j])
+    qidx = 2
+    p = orc.make_params(green_func_delt=0.2721, ecut_for_eps=2.5, em=em, dump_chi=1, nthreads=2, fft_box=box,
+                        calc_num_k=[qidx])
+    orc.calc_chiqw(root, p)
+    chi = orc.read_chi_dump(os.path.join(root, "dir-eps", "q%03d" % qidx, "dat.chi0"))[..., 0]
+    imt = orc.mkidx(spec.nk, d.bvec)
+    ref, LG = brute.chi0_brute(d, d.kpts[qidx - 1], 2.5, em, 0.2721, 0.001, 0.001, spec.nbands,
+                               (list(range(spec.nocc)), list(range(spec.nocc, spec.nbands))),
+                               imt1=imt, nk=spec.nk, tetra=_tetra_fn(spec.nk, imt, d.efermi, 0.2721 / AU, em))
+    assert chi.shape == ref.shape and chi.shape[0] > 5
+    err = np.abs(chi - ref).max() / np.abs(ref).max()
+    assert err < 1e-6, err
+
+
 def test_eps_files_invert_chi(case_dir, fresh_copy):
     """dat.epsqw.600 holds (1 - v chi_total)^-1 of the dumped chi (q != 0) and
     the diagonal text file matches it."""
