@@ -58,8 +58,10 @@ typedef struct rp_params {
   int    qshard_count;         /* number of shards (1 = all q here)          */
   int    pair_fp64;            /* tensor-core precisions: pair densities in FP64
                                   (as the reference) instead of FP32          */
-  int    tc_ksub;              /* K blocks (of 64) per FP32 accumulation before
-                                  the FP64 reduction (0 = default)            */
+  int    tc_ksub;              /* K blocks (of 64) per FP32 accumulation in
+                                  tensor memory before it joins the float-pair
+                                  sums (0 = 16; at most 16 for the three-plane
+                                  precisions, whose integer sums stay exact)  */
   int    pair_batch;           /* at most this many band pairs per batch of a
                                   q (0 = as many as fit in 24 GB)             */
   int    tc_split;             /* K splits of the tensor-core Gram launch (0 =
