@@ -1,0 +1,101 @@
+// rp_tetra_series.cuh -- well-conditioned vertex weights of one tetrahedron,
+// FP32, for host and device.
+//
+// For a tetrahedron with linear g (vertex values g_v = dsgn (gr_v + i delt),
+// all with the same imaginary part), the linear-tetrahedron weight of vertex v
+// for frequency w is a confluent divided difference.  The closed forms of
+// m_tetrahedron_20170325.F:304-451 (sub2normal / sub1normal) evaluate it as
+// sums of terms g^2 log g / prod(g_i - g_j).  Those terms cancel by up to
+// (|w + g| / |g_i - g_j|)^3, which costs FP64 about 1e-6 of the per-k weights
+// on dense meshes.  Expanded about the mean gbar instead:
+//   c_v = sum_n (-1)^n n!/(n+4)! h_n(d_0..d_3, d_v) / z^(n+1),
+//   z = w + gbar,  d_i = g_i - gbar (real),
+// where h_n is the complete homogeneous polynomial of degree n in the five
+// values d_0..d_3 and d_v again.  The terms fall off like r^n with
+// r = max|d| / |z|.  For r <= 0.5 the series in FP32 is closer to the exact
+// weights than the closed forms in FP64.  Larger r (near resonance) is left
+// to the closed forms, which are well conditioned there.
+//
+// The h_n are generated in ascending n by the recurrences
+//   H1_n = d0 H1_{n-1},  Hm_n = H(m-1)_n + d(m-1) Hm_{n-1}  (m = 2..4),
+//   Hv_n = H4_n + d_v Hv_{n-1},
+// so no arrays are kept: eight running values and four complex sums.
+#pragma once
+
+#include <math.h>
+
+#if defined(__CUDACC__)
+#define RP_TS_HD __host__ __device__ __forceinline__
+#else
+#define RP_TS_HD inline
+#endif
+
+namespace rp {
+
+struct TsCplx {
+  float r, i;
+};
+
+// the largest r the series takes, and its term cap
+constexpr float TS_RMAX = 0.5f;
+constexpr int TS_NMAX = 30;
+
+// Vertex weights x[v] (v = 0..3, the order of gr) of one tetrahedron for one
+// sign (dsgn = +-1) and frequency w = (wr, wi), in the closed forms'
+// normalisation (all four equal: x = 1 / (24 (w + g))).  Returns false, with x
+// untouched, when r > TS_RMAX or z = 0.
+RP_TS_HD bool tetra_series_weights(const double (&gr)[4], double dsgn, double delt, double wr, double wi,
+                                   TsCplx (&x)[4]) {
+  const double mean = 0.25 * ((gr[0] + gr[1]) + (gr[2] + gr[3]));
+  // z = w + gbar in double (one subtraction's worth of care), the rest in FP32
+  const double zr = wr + dsgn * mean, zi = wi + dsgn * delt;
+  const double zz = zr * zr + zi * zi;
+  if (!(zz > 0.0)) return false;
+  float d[4];
+  float dmax = 0.f;
+  for (int v = 0; v < 4; v++) {
+    d[v] = (float)(dsgn * (gr[v] - mean));
+    dmax = fmaxf(dmax, fabsf(d[v]));
+  }
+  const float r = dmax / (float)sqrt(zz);
+  if (!(r <= TS_RMAX)) return false;
+  // terms to FP32 rounding: term n is at most r^n times the first
+  // (a_n h_n <= max|d|^n / 24), so r^N <= 2^-24 suffices
+  int nterm = 1;
+  if (r > 1e-30f) {
+    const float n = 1.f + ceilf(-24.f * 0.6931472f / logf(r));
+    nterm = n < (float)TS_NMAX ? (int)n : TS_NMAX;
+  }
+  // u = 1 / z
+  const float ur = (float)(zr / zz), ui = (float)(-zi / zz);
+  float h1 = 1.f, h2 = 1.f, h3 = 1.f, h4 = 1.f;   // H1_0 .. H4_0
+  float hv[4] = {1.f, 1.f, 1.f, 1.f};
+  float sr[4], si[4];
+  // n = 0: a_0 = 1/24, u^1
+  float pr = ur, pi = ui;                           // u^(n+1)
+  float an = 1.f / 24.f;
+  for (int v = 0; v < 4; v++) {
+    sr[v] = an * pr;
+    si[v] = an * pi;
+  }
+  for (int n = 1; n < nterm; n++) {
+    h1 = d[0] * h1;
+    h2 = h1 + d[1] * h2;
+    h3 = h2 + d[2] * h3;
+    h4 = h3 + d[3] * h4;
+    an = -an * (float)n / (float)(n + 4);
+    const float qr = pr * ur - pi * ui, qi = pr * ui + pi * ur;
+    pr = qr;
+    pi = qi;
+    for (int v = 0; v < 4; v++) {
+      hv[v] = h4 + d[v] * hv[v];
+      const float t = an * hv[v];
+      sr[v] += t * pr;
+      si[v] += t * pi;
+    }
+  }
+  for (int v = 0; v < 4; v++) x[v] = TsCplx{sr[v], si[v]};
+  return true;
+}
+
+}  // namespace rp
