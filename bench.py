@@ -7,19 +7,22 @@ dielectric cutoff 11 Ry (~600 G), 20 frequencies (10 real 0-30 eV, 10
 imaginary on a Gauss-Legendre grid over 0-30 eV), band-cRPA window 9-11.
 
 A step is one q point: rp_chi0_q (tetrahedron weights, pair densities,
-contraction) + rp_epsinv_q (eps build and FP64 inversion).  `value` is the
-device time per q point of the split-precision (FP16x3) path with every input
-resident in HBM; `e2e` is the same through the C ABI with host output
-buffers (chi and eps^-1 copied back every step).  Inputs (38 GB of real-space
-wave functions, 3.8 GB of pair densities per q) are larger than L2, so no
-flush is needed.  The plain FP64 GPU path and its chi error are measured on a
-1/16 band-pair sample of one q and scaled linearly in the pair count (every
-stage but the eps inversion is linear in it).  The CPU baseline is the C
-restatement (oracle) on the host cores on a bounded pair sample, scaled the
-same way.
+contraction) + rp_epsinv_q (eps build and inversion: FP32 Gauss-Jordan plus
+one float-pair Newton step, the FP64 Gauss-Jordan as fallback).  `value` is
+the device time per q point of the split-precision (FP16x3) path with every
+input resident in HBM; `e2e` is the same q points again through the C ABI
+with host output buffers (chi and eps^-1 copied back every step).  Inputs
+(38 GB of real-space wave functions, 3.8 GB of pair densities per q) are
+larger than L2, so no flush is needed.  The plain FP64 GPU path and the chi
+and eps^-1 errors of the fast path are measured on a 96-pair sample of the
+first timed q and scaled linearly in the pair count (every stage but the eps
+inversion is linear in it).  The CPU baseline is the C restatement (oracle)
+on the host cores on a bounded sample (pairs and k points), scaled the same
+way.  The default line also carries the ragged-batch leg (`ragged`).
 
---impl reference runs that CPU restatement as the reference arm: the
-reference (Fortran + MPI + MKL) cannot be built here (no Fortran compiler).
+--impl reference runs that CPU restatement as the reference arm on the GPU
+arm's timed q points: the reference (Fortran + MPI + MKL) cannot be built
+here (no Fortran compiler).
 """
 from __future__ import annotations
 
@@ -46,13 +49,9 @@ METRIC = "chiqw s/q-point (all w) vs plain FP64 GPU at chi rel err<=1e-6; % roof
 
 def make_spec(case="full"):
     from respackdev_gb300 import synth
-    if case == "small":
-        # the same cell, cutoffs, FFT box and frequencies on a 4x4x4 mesh with 100
-        # bands: the kernels of the full workload at a size an ncu capture can hold
-        return synth.SynthSpec(lattice="fcc", a=15.84, nk=(4, 4, 4), nbands=100, nocc=8, ecut_psi=20.0,
-                               seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False)
-    return synth.SynthSpec(lattice="fcc", a=15.84, nk=(8, 8, 8), nbands=200, nocc=8, ecut_psi=20.0,
-                           seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False)
+    # small: the same cell, cutoffs, FFT box and frequencies on a 4x4x4 mesh with
+    # 100 bands -- the kernels of the full workload at a size an ncu capture can hold
+    return synth.CASES["headline_small" if case == "small" else "headline"]
 
 
 def frequencies():
@@ -149,57 +148,90 @@ def profile_traffic():
     return None
 
 
-def cpu_baseline(root, nthreads, npair_sample, em, iq=2):
-    """The C restatement on host cores: one q, the first npair_sample pairs,
-    scaled to the full pair count."""
+def cpu_baseline(root, nthreads, npair_sample, em, iq, max_k=0):
+    """The C restatement on host cores, one q point on a bounded sample: the
+    first npair_sample band pairs, and with max_k > 0 their pair densities and
+    contraction over the first max_k k points only.  The time is scaled
+    linearly to all pairs and all k (the per-pair tetrahedron weights, under
+    0.5 % of a pair's time, always run over the whole mesh)."""
     from oracle import oracle as orc
     orc.build()
     shutil.rmtree(os.path.join(root, "dir-eps"), ignore_errors=True)
     p = orc.make_params(em=em, nthreads=nthreads, max_pairs=npair_sample, calc_num_k=[iq], fft_box=FFT_BOX,
-                        write_eps=0, **RUN_PARAMS)
+                        write_eps=0, max_k=max_k, **RUN_PARAMS)
     rep = orc.calc_chiqw(root, p)
-    frac = rep.npair_full_last / max(1, rep.npair_last)
+    frac = rep.npair_full_last / max(1, rep.npair_last) * rep.ntk / max(1, rep.nk_used_last)
     return rep.seconds_last_q * frac, rep
 
 
-def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    nthreads = os.cpu_count() or 1
-    tmp = tempfile.mkdtemp(prefix="rp_bench_ref_")
-    try:
-        prepare(tmp)
-        em = frequencies()
-        for _ in range(args.warmup):
-            cpu_baseline(tmp, nthreads, nthreads, em)
-        vals = []
-        t0 = time.time()
-        for _ in range(args.steps):
-            v, rep = cpu_baseline(tmp, nthreads, nthreads, em)
-            vals.append(v)
-        wall = time.time() - t0
-        value = float(np.mean(vals))
-        line = {"metric": METRIC, "value": value, "unit": "s/q-point", "impl": "reference",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
-                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": WORKLOAD, "ntk": rep.ntk, "nbands": make_spec().nbands,
-                           "npair": rep.npair_full_last, "ng": rep.ng_last, "nen": rep.nen,
-                           "fft_box": list(rep.fft_box), "parallelism": "openmp-host"},
-                "cpu_baseline": {"value": value, "unit": "s/q-point", "cores": nthreads, "kind": "port",
-                                 "sample": f"one q point, {rep.npair_last} of {rep.npair_full_last} band pairs, "
-                                           f"scaled linearly in the pair count (C restatement of chiqw; the Fortran "
-                                           f"reference cannot be built here)"},
-                "e2e": {"value": value, "unit": "s/q-point", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line), flush=True)
-    finally:
-        shutil.rmtree(tmp, ignore_errors=True)
+def num_qirr(root):
+    with open(os.path.join(root, "dir-wfn", "dat.sample-k")) as f:
+        return int(f.readline().split()[0])
 
 
 def shard_q(nq_all: int, rank: int, world: int):
     """q points of one rank: every world-th point after Gamma (weak scaling;
     the reference's MPI_num_qcomm q communities, chiqw.F:662-687)."""
     return list(range(2, nq_all + 1))[rank::world]
+
+
+def step_q_list(nq_all, rank, world, warmup, steps):
+    """The q point of every warm-up and timed step of one rank (cycling if needed)."""
+    mine = shard_q(nq_all, rank, world)
+    need = warmup + steps
+    return (mine * (need // max(1, len(mine)) + 1))[:need]
+
+
+def workload_config(ntk, nbands, npair, ng, nen, box, qs, world):
+    """`config` of both arms: the same workload keys and values."""
+    return {"workload": WORKLOAD, "ntk": ntk, "nbands": nbands, "npair": npair, "ng": ng, "nen": nen,
+            "fft_box": list(box), "q_points": f"{qs[0]}-{qs[-1]}" if qs else "",
+            "l2": "inputs larger than L2 (38 GB wave functions, 3.8 GB pair densities per q)",
+            "parallelism": f"q-shard x{world}"}
+
+
+def run_reference(args):
+    """The reference arm: the C restatement of chiqw on the host cores, each
+    step one timed q point of the GPU arm's list (a bounded sample of it:
+    as many band pairs as threads, over a quarter of the k mesh, scaled
+    linearly)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    nthreads = os.cpu_count() or 1
+    tmp = tempfile.mkdtemp(prefix="rp_bench_ref_")
+    try:
+        prepare(tmp)
+        em = frequencies()
+        qs = step_q_list(num_qirr(tmp), 0, world, args.warmup, args.steps)
+        ntk = int(np.prod(make_spec().nk))
+        for iq in qs[: args.warmup]:
+            cpu_baseline(tmp, 1, 1, em, iq, max_k=8)
+        vals, ngs = [], []
+        rep = None
+        t0 = time.time()
+        for iq in qs[args.warmup:]:
+            v, rep = cpu_baseline(tmp, nthreads, nthreads, em, iq, max_k=max(1, ntk // 4))
+            vals.append(v)
+            ngs.append(rep.ng_last)
+        wall = time.time() - t0
+        value = float(np.mean(vals))
+        line = {"metric": METRIC, "value": value, "unit": "s/q-point", "impl": "reference",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(rep.ntk, make_spec().nbands, rep.npair_full_last, ngs[0], rep.nen,
+                                          rep.fft_box, qs[args.warmup:], world),
+                "ng_per_step": ngs,
+                "cpu_baseline": {"value": value, "unit": "s/q-point", "cores": nthreads, "kind": "port",
+                                 "sample": f"per step one q point of the GPU arm's timed list, {rep.npair_last} of "
+                                           f"{rep.npair_full_last} band pairs over {rep.nk_used_last} of {rep.ntk} "
+                                           f"k points, scaled linearly (C restatement of chiqw on {nthreads} threads; "
+                                           f"the Fortran reference cannot be built here)"},
+                "e2e": {"value": value, "unit": "s/q-point", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def normwise(a, b):
@@ -232,12 +264,12 @@ def run_gpu(args):
         ctx = rp.Context(tmp, params, em)
         t_setup = time.time() - t0
         info = ctx.info()
-        nq_all = ctx.L.rp_num_qirr(ctx._h)
+        npair_full = info.n_occ * info.n_vir
+        K = npair_full * info.ntk
         # q points of this rank (weak scaling: every rank takes its own q points), Gamma excluded
-        mine = shard_q(nq_all, rank, world)
-        need = args.warmup + args.steps
-        mine = (mine * (need // max(1, len(mine)) + 1))[:need]
-        for iq in mine[: args.warmup]:
+        qs = step_q_list(ctx.L.rp_num_qirr(ctx._h), rank, world, args.warmup, args.steps)
+        timed = qs[args.warmup:]
+        for iq in qs[: args.warmup]:
             ctx.chi0_q(iq, fetch=False)
             ctx.epsinv_q(fetch=False)
         # --- device-resident timing ---
@@ -246,95 +278,108 @@ def run_gpu(args):
             dist.barrier()
         stage = np.zeros(5)
         tcg = 0.0
+        alg_flops = 0.0
+        ngs = []
         with ClockSampler(dev) as clk:
             t0 = time.perf_counter()
-            for iq in mine[args.warmup:]:
+            for iq in timed:
                 ctx.chi0_q(iq, fetch=False)
                 st1 = ctx.stage_times()
                 ctx.epsinv_q(fetch=False)
                 st2 = ctx.stage_times()
                 stage += np.array([st1[0], st1[1], st1[2], st2[3], st1[4]])
                 tcg += ctx.tc_gram_seconds()
+                ngs.append(ctx.ng)
             elapsed = time.perf_counter() - t0
         launches = ctx.kernel_launches() - launches0
+        for ng_q in ngs:
+            alg_flops += 8.0 * ng_q * ng_q * K * info.nen
         if dist:
             import torch
             t = torch.tensor([elapsed], dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             elapsed = float(t.item())
         value = elapsed / (args.steps * world)
-        # --- end to end through the C ABI with host buffers ---
-        ng, nen = ctx.ng, info.nen
-        e2e_steps = max(1, min(args.steps, 3))
+        # --- end to end through the C ABI with host buffers, the same timed q points ---
         h2d0, d2h0 = ctx.transfer_bytes()
         t0 = time.perf_counter()
-        for iq in mine[args.warmup: args.warmup + e2e_steps]:
+        for iq in timed:
             ctx.chi0_q(iq, fetch=True)
             ctx.epsinv_q(fetch=True)
-        e2e = (time.perf_counter() - t0) / e2e_steps
+        e2e = (time.perf_counter() - t0) / args.steps
         h2d1, d2h1 = ctx.transfer_bytes()
-        h2d, d2h = (h2d1 - h2d0) // e2e_steps, (d2h1 - d2h0) // e2e_steps
-        # --- plain FP64 path and the error of the fast path on a pair sample of one q ---
-        npair_full = info.n_occ * info.n_vir
-        iq0 = mine[args.warmup]
-        plain = err = None
+        h2d, d2h = (h2d1 - h2d0) // args.steps, (d2h1 - d2h0) // args.steps
+        ctx.close()
+        # --- plain FP64 path and the errors of the fast path on a pair sample of one q ---
+        iq0 = timed[0]
+        plain = err = eps_err = inv_err = None
         sample_pairs = 96
         if not args.no_plain:
-            pf = rp.default_params(precision=rp.PREC_FP64, fft_box=FFT_BOX, device=dev, max_pairs=sample_pairs,
-                                   **RUN_PARAMS)
-            with rp.Context(tmp, pf, em) as c64:
+            base = dict(fft_box=FFT_BOX, device=dev, max_pairs=sample_pairs, **RUN_PARAMS)
+            with rp.Context(tmp, rp.default_params(precision=rp.PREC_FP64, **base), em) as c64:
                 chi64 = c64.chi0_q(iq0)
                 s64 = c64.stage_times()
-                c64.epsinv_q(fetch=False)
+                eps64 = c64.epsinv_q()
                 e64 = c64.stage_times()[3]
-            ps = rp.default_params(precision=rp.PREC_FP16X3, fft_box=FFT_BOX, device=dev, max_pairs=sample_pairs,
-                                   **RUN_PARAMS)
-            with rp.Context(tmp, ps, em) as cs:
+            with rp.Context(tmp, rp.default_params(precision=rp.PREC_FP16X3, **base), em) as cs:
                 chis = cs.chi0_q(iq0)
+                epss = cs.epsinv_q()
+            with rp.Context(tmp, rp.default_params(precision=rp.PREC_FP16X3, eps_fp64=1, **base), em) as cf:
+                cf.chi0_q(iq0, fetch=False)
+                epsf = cf.epsinv_q()
             err = normwise(chis, chi64)
+            eps_err = normwise(epss, eps64)
+            inv_err = normwise(epss, epsf)
             plain = s64[4] * npair_full / sample_pairs + e64
         # --- roofline of the tensor-core contraction ---
         tflops_sus, tflops_burst, hbm, src = measured_peaks()
-        K = npair_full * info.ntk
-        alg_flops_per_q = 8.0 * ng * ng * K * nen
-        achieved = alg_flops_per_q * args.steps / tcg / 1e12 if tcg > 0 else None
+        achieved = alg_flops / tcg / 1e12 if tcg > 0 else None
         roof = {"bound": "tensor", "kernel": "tc_gram_kernel", "achieved": achieved, "peak": tflops_sus,
                 "unit": "TFLOP/s", "frac": (achieved / tflops_sus) if achieved else None,
                 "peak_source": f"{src} bf16 sustained", "traffic": profile_traffic(),
                 "tensor_products_per_real_product": 6,
                 "achieved_tensor_tflops": achieved * 6 if achieved else None,
-                "algorithmic_flops_per_q": alg_flops_per_q}
+                "algorithmic_flops_per_q": alg_flops / max(1, len(ngs)),
+                "algorithmic_flops": "8 NG^2 K nen per q, each q's own NG, K = pairs x k"}
         # --- CPU baseline (rank 0, host cores, bounded sample) ---
         cpu = None
         if rank == 0 and not args.no_cpu and args.case == "full":
             nthr = os.cpu_count() or 1
-            v, rep = cpu_baseline(tmp, nthr, nthr, em, iq=iq0)
+            v, rep = cpu_baseline(tmp, nthr, nthr, em, iq0, max_k=max(1, info.ntk // 4))
             cpu = {"value": v, "unit": "s/q-point", "cores": nthr, "kind": "port",
-                   "sample": f"one q point, {rep.npair_last} of {rep.npair_full_last} band pairs on {nthr} threads, "
-                             f"scaled linearly in the pair count"}
+                   "sample": f"q {iq0}, {rep.npair_last} of {rep.npair_full_last} band pairs over {rep.nk_used_last} "
+                             f"of {rep.ntk} k points on {nthr} threads, scaled linearly"}
         clocks = clk.summary()
+        ragged = None
+        if rank == 0 and args.case == "full" and not args.no_ragged:
+            ragged = run_ragged(args, steps=min(args.steps, 3), warmup=1, emit=False)
         if rank == 0:
             line = {"metric": METRIC,
                     "value": value, "unit": "s/q-point", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                     "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": False, "scaling": "weak",
                     "vs_baseline": None, "dtype": "fp16x3-split tensor contraction, f32 pair densities, f64 weights/eps",
                     "data": "synthetic (seeded generator, dir-wfn files)",
-                    "config": {"workload": WORKLOAD if args.case == "full" else WORKLOAD + "_small", "ntk": info.ntk, "nbands": info.ncb, "npair": npair_full,
-                               "npw_max": info.ntg, "ng": ng, "nen": nen, "fft_box": list(info.fft_box),
-                               "l2": "inputs larger than L2 (38 GB wave functions, 3.8 GB pair densities per q)",
-                               "parallelism": f"q-shard x{world}"},
+                    "config": workload_config(info.ntk, info.ncb, npair_full, ngs[0], info.nen, info.fft_box, timed,
+                                              world) | ({} if args.case == "full" else {"workload": WORKLOAD + "_small"}),
+                    "ng_per_step": ngs, "npw_max": info.ntg,
                     "plain_fp64_s_per_q": plain, "speedup_vs_plain_fp64": (plain / value) if plain else None,
                     "plain_fp64_sample": f"{sample_pairs} of {npair_full} pairs on q {iq0}, scaled linearly",
+                    "plain_fp64_note": "the plain FP64 kernel forms the full complex chi (8 real flops per G, G', "
+                                       "K, w); the split path forms the upper halves of two real symmetric Gram "
+                                       "matrices of size 2 NG per w (also 8 NG^2 real flops per K and w), so both "
+                                       "do the algorithmic count",
                     "chi_rel_err_vs_fp64": err,
+                    "epsinv_rel_err_vs_fp64": eps_err,
+                    "epsinv_mixed_vs_fp64_inverse_same_chi": inv_err,
                     "stage_seconds_per_q": {"tetra": stage[0] / args.steps, "pair_density": stage[1] / args.steps,
                                             "contraction": stage[2] / args.steps, "eps_inverse": stage[3] / args.steps},
                     "setup_seconds": t_setup, "input_generation_seconds": t_prep,
                     "roofline": roof, "clocks": clocks,
                     "e2e": {"value": e2e, "unit": "s/q-point", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                            "note": "wave functions uploaded once per run (setup_seconds)"},
-                    "gpu_launches": launches, "cpu_baseline": cpu}
+                            "note": "all timed q points again through the C ABI with host result buffers; "
+                                    "wave functions uploaded once per run (setup_seconds)"},
+                    "gpu_launches": launches, "cpu_baseline": cpu, "ragged": ragged}
             print(json.dumps(line), flush=True)
-        ctx.close()
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
         if dist:
@@ -387,11 +432,14 @@ def _make_cell(args):
     return root
 
 
-def run_ragged(args):
+def run_ragged(args, steps=None, warmup=None, emit=True):
     """One step = chi0 of every problem of the ragged workload (two q points of
     each of the 12 cells) through rp_chi0_batch: preparation per problem, one
     grouped tensor-core launch and the assembly in one CUDA graph.  The same
-    problems through rp_chi0_q one by one are timed beside it."""
+    problems through rp_chi0_q one by one are timed beside it.  Prints the
+    line (emit) and returns it."""
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     import concurrent.futures as cf
     import multiprocessing as mp
     tmp = tempfile.mkdtemp(prefix="rp_ragged_")
@@ -401,8 +449,8 @@ def run_ragged(args):
         for r in roots:
             os.makedirs(r)
         t0 = time.time()
-        # generate the cells in spawned processes before any GPU call, one BLAS
-        # thread each (the workers inherit the environment at spawn)
+        # generate the cells in spawned processes (safe after GPU calls, unlike
+        # forked ones), one BLAS thread each (the workers inherit the environment)
         blas = ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS")
         saved = {k: os.environ.get(k) for k in blas}
         os.environ.update({k: "1" for k in blas})
@@ -434,39 +482,41 @@ def run_ragged(args):
                 shapes.append({"cell": i, "lattice": spec.lattice, "a": round(spec.a, 3), "nk": spec.nk[0],
                                "bands": spec.nbands, "npw_max": inf.ntg, "q": iq, "ng": ng, "ndir": nd,
                                "nen": inf.nen, "npair": inf.n_occ * inf.n_vir})
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(1, warmup)):
             rp.chi0_batch(probs, graph=True, fetch=False)
         launches0 = sum(c.kernel_launches() for c in ctxs)
         t0 = time.perf_counter()
         secs = np.zeros(3)
-        for _ in range(args.steps):
+        for _ in range(steps):
             _, s = rp.chi0_batch(probs, graph=True, fetch=False)
             secs += s
-        batch = (time.perf_counter() - t0) / args.steps
-        launches = (sum(c.kernel_launches() for c in ctxs) - launches0) // args.steps
+        batch = (time.perf_counter() - t0) / steps
+        launches = (sum(c.kernel_launches() for c in ctxs) - launches0) // steps
         t0 = time.perf_counter()
         seq_gram = 0.0
-        for _ in range(args.steps):
+        for _ in range(steps):
             for c, iq in probs:
                 c.chi0_q(iq, fetch=False)
                 seq_gram += c.tc_gram_seconds()
-        seq = (time.perf_counter() - t0) / args.steps
-        seq_gram /= args.steps
+        seq = (time.perf_counter() - t0) / steps
+        seq_gram /= steps
         n = len(probs)
         line = {"metric": "chiqw ragged batch s/problem (all w), 12 cells in one grouped launch",
-                "value": batch / n, "unit": "s/problem", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                "value": batch / n, "unit": "s/problem", "n_gpus": 1, "steps": steps, "warmup": warmup,
                 "higher_is_better": False, "dtype": "fp16x3-split tensor contraction, f32 pair densities",
                 "data": "synthetic (seeded generator, 12 cells)",
                 "config": {"workload": "chiqw_ragged_12cells", "problems": n, "cells": len(cells)},
                 "sequential_s_per_problem": seq / n, "speedup_vs_sequential": seq / batch,
                 "sequential_gram_device_seconds": seq_gram,
-                "batch_seconds": {"prepare": secs[0] / args.steps, "graph_device": secs[1] / args.steps,
-                                  "finish": secs[2] / args.steps},
+                "batch_seconds": {"prepare": secs[0] / steps, "graph_device": secs[1] / steps,
+                                  "finish": secs[2] / steps},
                 "gram_launches_per_batch": 1, "gpu_launches_per_batch": int(launches),
                 "tuned_shapes": rp.tuned_shapes(), "input_generation_seconds": gen, "shapes": shapes}
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
         for c in ctxs:
             c.close()
+        return line
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
 
@@ -479,6 +529,7 @@ def main():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-batch leg of the default line")
     ap.add_argument("--case", default="full", choices=["full", "small", "ragged"],
                     help="small: 4x4x4 k, 100 bands, same kernels (for profiler captures); "
                          "ragged: 12 cells' chi0 problems in one grouped launch")

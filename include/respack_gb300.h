@@ -69,6 +69,10 @@ typedef struct rp_params {
   int    write_eps_f32;        /* 1: rp_write_q also writes dat.epsqw.c4, the
                                   complex(4) eps^-1 calc_int reads (Gamma: the
                                   mean of the three directions)              */
+  int    eps_fp64;             /* 1: the split precisions also invert eps with
+                                  the FP64 Gauss-Jordan (0: FP32 Gauss-Jordan
+                                  plus one float-pair Newton step, FP64 only
+                                  as its fallback)                            */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */
@@ -241,24 +245,28 @@ int rp_calc_j3d(const char *root, const char *namelist_text);
 
 /* Batched inverse of nmat complex n x n matrices (column-major, interleaved
  * re/im doubles, matrix m at a + 2*m*n*n) that allocates no device memory.
- * No counterpart in the reference: it is the inversion step of rp_epsinv_q
- * (invZGE.F90:1-22, partial pivoting on |re|+|im|) offered on its own for
- * callers that cannot allocate GPU memory or let a library do so -- a Fortran
- * or C++ host whose device memory belongs to its own allocator or pool, or
- * code that runs where cudaMalloc is not allowed.  a and ainv are device
- * pointers, 16-byte aligned; a == ainv inverts in place, otherwise a is left
- * unchanged.  The work is queued on `stream` (a cudaStream_t, NULL = legacy
- * default stream) and the call returns after that stream has finished it.
+ * It has no counterpart in the reference.  It is the inversion step of
+ * rp_epsinv_q (partial pivoting on |re|+|im|) offered on its own for callers
+ * that cannot allocate GPU memory or let a library do so -- a Fortran or C++
+ * host whose device memory belongs to its own allocator or pool, or code that
+ * runs where cudaMalloc is not allowed.  a and ainv are device pointers,
+ * 16-byte aligned, either the same buffer (the inverse overwrites it) or not
+ * overlapping at all (a is left unchanged); a partial overlap is rejected.  The
+ * work is queued on `stream` (a cudaStream_t, NULL = legacy default stream) and
+ * the call synchronizes that stream before it returns.
  *
  * Scratch lives in one fixed device array of the library (about 4.6 MB per
- * GPU, allocated when the library is loaded): n*nmat <= 131072 and
- * nmat <= 1024, larger requests are rejected with code 1 before any work.
- * Nothing in it has to start at zero; the error word is cleared by each call.
- * The first call on each device looks the array up (cudaGetSymbolAddress) with
- * that device current; make it before any stream capture.  Calls whose work
- * overlaps on the GPU (different streams or host threads) share the array and
- * race: serialise them.  Returns 0, 1 (bad arguments or size), 3 (singular
- * matrix) or -1 (CUDA error); rp_last_error(NULL) gives the text. */
+ * GPU): n*nmat <= 131072 and nmat <= 1024, larger requests are rejected with
+ * code 1 before any work.  CUDA loads the library's device code lazily by
+ * default, so the array is reserved on a device at the first call there (or
+ * when the program starts, with CUDA_MODULE_LOADING=EAGER): make that first
+ * call before the host reserves its own pool.  Nothing in the array has to
+ * start at zero; the error word is cleared by each call.  The first call on
+ * each device also looks the array up (cudaGetSymbolAddress) with that device
+ * current; make it before any stream capture.  Calls whose work overlaps on the
+ * GPU (different streams or host threads) share the array and race: serialise
+ * them.  Returns 0, 1 (bad arguments or size), 3 (singular matrix) or -1 (CUDA
+ * error); rp_last_error(NULL) gives the text. */
 int rp_zinv_batched_noalloc(const double *a, double *ainv, int n, int nmat, void *stream);
 
 /* ---- band-tail MLP (no reference counterpart) ----------------------------

@@ -33,14 +33,14 @@ class Params(C.Structure):
         ("file_num_eps_start", C.c_int), ("file_num_eps_base_start", C.c_int), ("n_calc_q", C.c_int),
         ("calc_num_k", C.POINTER(C.c_int)), ("nen_explicit", C.c_int), ("em_explicit", C.POINTER(C.c_double)),
         ("fft_box", C.c_int * 3), ("dump_chi", C.c_int), ("write_eps", C.c_int), ("nthreads", C.c_int),
-        ("max_pairs", C.c_int), ("max_q", C.c_int),
+        ("max_pairs", C.c_int), ("max_q", C.c_int), ("max_k", C.c_int),
     ]
 
 
 class Report(C.Structure):
     _fields_ = [("nq_done", C.c_int), ("ntk", C.c_int), ("ng_last", C.c_int), ("npair_last", C.c_int),
                 ("npair_full_last", C.c_int), ("nen", C.c_int), ("fft_box", C.c_int * 3),
-                ("seconds_total", C.c_double), ("seconds_last_q", C.c_double)]
+                ("seconds_total", C.c_double), ("seconds_last_q", C.c_double), ("nk_used_last", C.c_int)]
 
 
 class IntParams(C.Structure):

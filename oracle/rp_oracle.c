@@ -1315,7 +1315,7 @@ typedef struct {
 
 static int pair_loop(const orc_state *s, const double *q, const int *LG0, int NG, int gamma, int No_G_0,
                      const int *ipair, const int *jpair, int npair, const int *kpq, const int *sG, cplx *chi,
-                     int nthreads) {
+                     int nthreads, int nk_use) {
     int ndir = gamma ? 3 : 1;
     int nen = s->nen, NTK = s->NTK;
     long chisz = (long)NG * NG * nen * ndir;
@@ -1348,7 +1348,7 @@ static int pair_loop(const orc_state *s, const double *q, const int *LG0, int NG
         for (int ij = lo; ij < hi && !err; ij++) {
             int ib = ipair[ij], jb = jpair[ij];          /* 0-based vir / occ index */
             int bandv = s->N_docc + ib, bando = jb;      /* absolute band (0-based) */
-            for (int ik = 0; ik < NTK; ik++) {
+            for (int ik = 0; ik < nk_use; ik++) {
                 int ikq = kpq[ik];
                 make_C0(s, ik, bando, b.C0K);
                 make_C0(s, ikq, bandv, b.C0KQ);
@@ -1395,7 +1395,7 @@ static int pair_loop(const orc_state *s, const double *q, const int *LG0, int NG
                             const cplx *ri = b.ism + ((long)ix * NG + ig) * NTK, *rj = b.ism + ((long)ix * NG + jg) * NTK;
                             const cplx *xw = b.xow + (long)e * NTK;
                             cplx sacc = b.pc[((long)ix * nen + e) * NG * NG + ig + (long)NG * jg];
-                            for (int ik = 0; ik < NTK; ik++) {
+                            for (int ik = 0; ik < nk_use; ik++) {
                                 int ikq = kpq[ik];
                                 cplx pp = 1.0 - s->prob[(long)ik * s->NTB + bando] * s->prob[(long)ikq * s->NTB + bandv];
                                 sacc = sacc + xw[ik] * conj(ri[ik]) * rj[ik] / (double)NTK * pp;
@@ -1511,7 +1511,8 @@ int orc_calc_chiqw(const char *root, const orc_params *P, orc_report *rep) {
         int ndir = gamma ? 3 : 1;
         long chisz = (long)NG * NG * s->nen * ndir;
         cplx *chi = malloc(sizeof(cplx) * chisz);
-        rc = pair_loop(s, q, LG0, NG, gamma, No_G_0, ip, jp, np, kpq, sG, chi, P->nthreads);
+        const int nk_use = (P->max_k > 0 && P->max_k < s->NTK) ? P->max_k : s->NTK;
+        rc = pair_loop(s, q, LG0, NG, gamma, No_G_0, ip, jp, np, kpq, sG, chi, P->nthreads, nk_use);
         /* intraband plasma frequency at Gamma (:1639-1733, :1989-1994) */
         double wd[3] = {0, 0, 0};
         if (!rc && gamma && nintra > 0) {
@@ -1600,6 +1601,7 @@ int orc_calc_chiqw(const char *root, const orc_params *P, orc_report *rep) {
             rep->nq_done++; rep->ntk = s->NTK; rep->ng_last = NG; rep->npair_last = np; rep->npair_full_last = npair_full;
             rep->nen = s->nen; rep->fft_box[0] = s->nw[0]; rep->fft_box[1] = s->nw[1]; rep->fft_box[2] = s->nw[2];
             rep->seconds_last_q = now_s() - tq;
+            rep->nk_used_last = nk_use;
         }
     }
     free(LG0); free(kpq); free(sG); free(ip); free(jp); free(qlist);

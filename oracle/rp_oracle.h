@@ -50,6 +50,9 @@ typedef struct orc_params {
     int    nthreads;               /* OpenMP threads (0 = runtime default)   */
     int    max_pairs;              /* >0: bounded sample of the first pairs (CPU timing) */
     int    max_q;                  /* >0: stop after this many q             */
+    int    max_k;                  /* >0: timing sample: pair densities and the
+                                      contraction over the first max_k k points
+                                      only (chi is then incomplete)            */
 } orc_params;
 
 /* Per-run timing/size report. */
@@ -59,6 +62,7 @@ typedef struct orc_report {
     int    fft_box[3];
     double seconds_total;
     double seconds_last_q;
+    int    nk_used_last;           /* k points of the pair densities and contraction */
 } orc_report;
 
 void orc_default_params(orc_params *p);

@@ -481,7 +481,8 @@ static void epsinv_run(rp_ctx *c) {
   for (int d = 0; d < 3; d++) a.wd[d] = c->wd[d];
   RP_CUDA(cudaEventRecord(c->ev[0], st));
   c->launches += rp::launch_eps_build(c->chi.as<double2>(), a, c->A.as<double2>(), st);
-  bool fp64 = c->S.params.precision == RP_PREC_FP64;
+  bool fp64 = c->S.params.precision == RP_PREC_FP64 || c->S.params.eps_fp64 != 0;
+  c->eps_fallback = false;
   if (!fp64) {
     // FP32 Gauss-Jordan plus one float-pair Newton step; its own singular flag and
     // per-matrix |R|_F^2 decide whether the FP64 inversion has to run instead

@@ -289,6 +289,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "pair_batch") p->pair_batch = nl_int(v, k);
       else if (k == "tc_split") p->tc_split = nl_int(v, k);
       else if (k == "write_eps_f32") p->write_eps_f32 = nl_int(v, k);
+      else if (k == "eps_fp64") p->eps_fp64 = nl_int(v, k);
       else if (k == "freq_re_ev") for (auto &x : v) fre.push_back(to_num(x));
       else if (k == "freq_im_ev") for (auto &x : v) fim.push_back(to_num(x));
       else fail(1, "namelist &param_gpu: unknown name '%s'", k.c_str());

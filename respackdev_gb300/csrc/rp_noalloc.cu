@@ -9,13 +9,18 @@
 // rp_epsinv_q) with its scratch -- pivot rows, pivot columns, pivot indices and
 // an error word -- in one file-scope device array of fixed size.
 //
-// The scratch array exists once per GPU that loads the library and stays
-// allocated until the process exits.  Every call shares it and it keeps the
-// last call's contents: the error word is cleared at the start of each call,
-// the other parts are fully rewritten before they are read.  Calls that overlap
-// on the GPU (on different streams or threads) race on it and give wrong
-// results.  The first call on a device looks up the array's device address
-// with cudaGetSymbolAddress; make that first call before any stream capture.
+// The scratch array exists once per GPU on which this file's device code is
+// loaded, and it stays allocated until the process exits.  CUDA loads modules
+// lazily by default, so the array is reserved at the first call on a device
+// (unless CUDA_MODULE_LOADING=EAGER): a host that hands all device memory to
+// its own pool should make that first call before it reserves the pool.
+// Every call shares the array and it keeps the last call's contents: the
+// error word is cleared at the start of each call, the other parts are fully
+// rewritten before they are read.  Calls that overlap on the GPU (on
+// different streams or threads) race on it and give wrong results.  The first
+// call on a device looks up the array's device address with
+// cudaGetSymbolAddress; make that first call before any stream capture.  Each
+// call waits for its stream to finish the work before it returns.
 #include <mutex>
 
 #include "rp_dev.cuh"
@@ -155,6 +160,13 @@ extern "C" int rp_zinv_batched_noalloc(const double *a, double *ainv, int n, int
       rp::fail(1, "rp_zinv_batched_noalloc: n*nmat = %ld exceeds the fixed scratch (n*nmat <= %d, nmat <= %d)",
                (long)n * nmat, kMaxRows, kMaxMats);
     if (((uintptr_t)a | (uintptr_t)ainv) & 15) rp::fail(1, "rp_zinv_batched_noalloc: buffers must be 16-byte aligned");
+    {
+      // the input and output must be the same buffer or not overlap at all
+      const uintptr_t lo_a = (uintptr_t)a, lo_b = (uintptr_t)ainv;
+      const uintptr_t len = (uintptr_t)sizeof(double2) * (uintptr_t)n * (uintptr_t)n * (uintptr_t)nmat;
+      if (lo_a != lo_b && lo_a < lo_b + len && lo_b < lo_a + len)
+        rp::fail(1, "rp_zinv_batched_noalloc: a and ainv overlap without being the same buffer");
+    }
     int dev = 0;
     RP_CUDA(cudaGetDevice(&dev));
     NoAllocScratch *s = scratch_for(dev);

@@ -397,4 +397,11 @@ CASES = {
                          wan_lo=5, wan_hi=6, nwf=2, wan_sigma=1.0),
     # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
     "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
+    # the 8x8x8-k / 200-band workload's cell, cutoffs and FFT box (fcc a=15.84,
+    # 20 Ry, 36^3 box, about 600 G at 11 Ry) on a 4x4x4 mesh with 100 bands
+    "headline_small": SynthSpec(lattice="fcc", a=15.84, nk=(4, 4, 4), nbands=100, nocc=8, ecut_psi=20.0,
+                                seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False),
+    # the 8x8x8-k / 200-band workload itself
+    "headline": SynthSpec(lattice="fcc", a=15.84, nk=(8, 8, 8), nbands=200, nocc=8, ecut_psi=20.0,
+                          seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False),
 }

@@ -104,3 +104,47 @@ def test_complex4_eps_side_file_gives_the_same_w(int_case, int_copy):
     assert np.array_equal(V0, V1) and np.array_equal(X0, X1)
     assert np.array_equal(W0, W1) and np.array_equal(J0, J1)
 
+
+
+def _def_entries(path):
+    """Header lines, then (integer index tokens, value) of every data line of a z*.def file."""
+    lines = open(path).read().splitlines()
+    head, rows = lines[:5], []
+    for ln in lines[5:]:
+        tok = ln.split()
+        if tok:
+            rows.append((tuple(int(x) for x in tok[:-1]), float(tok[-1])))
+    return head, rows
+
+
+def test_mvmc_files_match_oracle_writer(int_case, int_copy, tmp_path):
+    """dir-mvmc written by rp_calc_w3d + rp_calc_j3d against the oracle's
+    restatement of wrt_mvmc (wrt_mvmc_w3d.f90:1-147, wrt_mvmc_j3d.f90): the
+    same files, headers (counts and cuts) and site pairs, values within the
+    calc_int tolerance."""
+    import shutil
+    rp_build.build()
+    src = int_case("tiny_wan")
+    gpu_root = int_copy(src)
+    orc_root = str(tmp_path / "oracle_copy")
+    for sub in ("dir-wfn", "dir-wan", "dir-eps"):
+        shutil.copytree(os.path.join(src, sub), os.path.join(orc_root, sub))
+    nl = "&param_calc_int\n calc_ifreq=2, ix_intJ_min=0, ix_intJ_max=1, wcut_mvmc=0.5, jcut_mvmc=0.01 /\n"
+    for prog in ("rp_calc_w3d", "rp_calc_j3d"):
+        r = subprocess.run([os.path.join(rp_build.BINDIR, prog)], input=nl, text=True,
+                           cwd=gpu_root, capture_output=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+    orc.calc_int(orc_root, orc.make_int_params(nthreads=4, ix_min=0, ix_max=1, calc_ifreq=2, wcut_mvmc=0.5,
+                                               jcut_mvmc=0.01, write_files=1))
+    names = sorted(os.listdir(os.path.join(orc_root, "dir-mvmc")))
+    assert names == sorted(os.listdir(os.path.join(gpu_root, "dir-mvmc")))
+    assert len(names) == 5
+    for name in names:
+        h1, r1 = _def_entries(os.path.join(gpu_root, "dir-mvmc", name))
+        h2, r2 = _def_entries(os.path.join(orc_root, "dir-mvmc", name))
+        assert h1 == h2, name
+        assert [i for i, _ in r1] == [i for i, _ in r2], name
+        v1 = np.array([v for _, v in r1])
+        v2 = np.array([v for _, v in r2])
+        assert r2, name
+        assert np.abs(v1 - v2).max() <= TOL * np.abs(v2).max() + 1e-9, name

@@ -34,6 +34,9 @@ def test_noalloc_rejects_sizes_beyond_scratch():
     assert L.rp_zinv_batched_noalloc(fake, fake, 0, 4, None) == 1
     assert L.rp_zinv_batched_noalloc(None, fake, 4, 4, None) == 1
     assert b"null pointer" in L.rp_last_error(None)
+    # a partial overlap of input and output is rejected (4x4 complex = 256 bytes)
+    assert L.rp_zinv_batched_noalloc(fake, C.c_void_p(4096 + 128), 4, 1, None) == 1
+    assert b"overlap" in L.rp_last_error(None)
 
 
 def _eps_from_chi(chi: np.ndarray, ql: np.ndarray) -> np.ndarray:
