@@ -68,7 +68,8 @@ struct rp_ctx {
   long long launches = 0;
   int R[3]{};  // psi-sphere extent per dimension
   // persistent device data
-  DevBuf coef, numirr, trs, src, phase, ng0, kg0, cfull, ur, energy, prob, imt1, index2, em, b9, sk0, errw;
+  DevBuf coef, numirr, trs, src, phase, ng0, kg0, cfull, ur, energy, prob, imt1, index2, em, b9, sk0, errw, inc_off,
+      inc;
   // per-q device data
   DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
       rowcol, A, eps, prow, fcol, piv, used, intra, pwpl, mixws, mixaux;
@@ -87,7 +88,7 @@ struct rp_ctx {
   long long h2d = 0, d2h = 0;  // bytes moved between host and device by this context's calls
   ~rp_ctx() {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
-                      &b9, &sk0, &errw, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
+                      &b9, &sk0, &errw, &inc_off, &inc, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
                       &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
                       &intra, &pwpl, &mixws, &mixaux})
       b->release();
@@ -132,6 +133,7 @@ static void check_device_error(rp_ctx *c) {
   if (e == 2) rp::fail(-3, "tetrahedron degeneracy classification failed (bad i3 / bad sum ia2)");
   if (e == 3) rp::fail(-3, "dielectric matrix is singular");
   if (e == 4) rp::fail(-3, "tensor-core contraction: wait limit reached");
+  if (e == 5) rp::fail(-3, "a tetrahedron is cut by the Fermi level although no band is partially occupied");
 }
 
 static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const double *em, int nen_explicit) {
@@ -164,6 +166,17 @@ static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const do
   upload(c->energy, S.e_eigi, st);
   upload(c->prob, S.prob, st);
   upload(c->imt1, S.imt1, st);
+  {
+    // the tetrahedra around each mesh slot (4*tetrahedron + vertex position), for
+    // the gathered weights of the split precisions
+    std::vector<int> off(S.ntk + 1, 0), inc(S.imt1.size());
+    for (int sl : S.imt1) off[sl + 1]++;
+    for (int m = 0; m < S.ntk; m++) off[m + 1] += off[m];
+    std::vector<int> fill(off.begin(), off.end() - 1);
+    for (size_t i = 0; i < S.imt1.size(); i++) inc[fill[S.imt1[i]]++] = (int)i;
+    upload(c->inc_off, off, st);
+    upload(c->inc, inc, st);
+  }
   std::vector<int> idx2(S.index_kpt);
   idx2.insert(idx2.end(), S.mesh_of_k.begin(), S.mesh_of_k.end());
   upload(c->index2, idx2, st);
@@ -319,9 +332,12 @@ static void q_batch(rp_ctx *c, QRun &r, int bi, rp::TcWorkspace *ws, bool run_gr
   ta.prob = c->prob.as<double2>(); ta.em = c->em.as<double2>(); ta.pair_vir = c->pvir.as<int>();
   ta.pair_occ = c->pocc.as<int>(); ta.npair = nb; ta.efermi = S.efermi; ta.delt = S.delt; ta.dmna = S.dmna;
   ta.dmnr = S.dmnr; ta.err = c->errw.as<int>();
+  ta.inc_off = c->inc_off.as<int>(); ta.inc = c->inc.as<int>(); ta.may_cut = S.n_pocc > 0 ? 1 : 0;
   c->wts.ensure(sizeof(cd) * (size_t)nb * nen * ntk);
   RP_CUDA(cudaEventRecord(c->ev[0], st));
-  c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st);
+  // the split precisions take the FP32 series where it converges; the plain
+  // FP64 path keeps the reference's closed forms everywhere
+  c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st, r.fast);
   RP_CUDA(cudaEventRecord(c->ev[1], st));
   rp::PairGeom pg;
   pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;

@@ -120,8 +120,17 @@ struct TetraArgs {
   int npair;
   double efermi, delt, dmna, dmnr;
   int *err;               // device error word
+  // the FP32-series kernel: tetrahedra around each mesh slot (CSR: slot m owns
+  // inc[inc_off[m] .. inc_off[m+1]), entries 4*tetrahedron + vertex position),
+  // and whether any tetrahedron can be cut by the Fermi level (a partially
+  // occupied band exists)
+  const int *inc_off = nullptr, *inc = nullptr;
+  int may_cut = 1;
 };
-int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st);
+// series = false: the reference's closed forms in FP64 for every tetrahedron
+// (the plain FP64 path); true: the FP32 series wherever it converges, the
+// closed forms in FP64 elsewhere (the split-precision paths)
+int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st, bool series = false);
 // Intraband plasma frequency at Gamma (ttrhdrn_simple + calc_VMaa): accumulates
 // pwpl[3] (complex) for each band in bands[].
 int launch_intraband(const TetraArgs &a, const double2 *cfull, const int *ng0, const int *kg0, int ncb,

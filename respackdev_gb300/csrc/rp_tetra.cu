@@ -14,6 +14,7 @@
 // Fermi level does not cut (all of them for an insulator) skip ttct.
 #include "rp_dev.cuh"
 #include "rp_host.h"
+#include "rp_tetra_series.cuh"
 
 namespace rp {
 
@@ -343,120 +344,19 @@ __device__ __forceinline__ void normal_terms(const NormalCoef &c, double sg, con
   x[0] = (F4 - F2 - F1 - F0) * sg;
 }
 
-// Near-degenerate, uncut tetrahedra with shared logs.  The reference's special
-// forms (sub1g30g21 ... sub2simple, m_tetrahedron_20170325.F:304-451) are
-// evaluated at points that all share the imaginary part delt*dsgn -- the
-// vertices and the averages geq of the degenerate ones -- so every energy
-// difference is real and log(z_a / z_b) = L_a - L_b.  Vertex logs come from
-// the shared table; only the averages need a log of their own.
-struct Pt { double g; cx Z, L; };  // real part of g, z = g + w, log z
-
-__device__ __forceinline__ cx f_s1g30g21(const Pt &p0, const Pt &p1) {
-  const double d = p0.g - p1.g;
-  return (0.5 * (p0.Z + p1.Z)) / (d * d) - (p0.L - p1.L) * p0.Z * p1.Z / (d * d * d);
-}
-__device__ __forceinline__ cx f_s1g30g20(const Pt &p0, const Pt &p1) {
-  const double d = p0.g - p1.g;
-  return (p0.Z - 3.0 * p1.Z) * 0.25 / (d * d) + p1.Z * p1.Z * (p0.L - p1.L) * 0.5 / (d * d * d);
-}
-__device__ __forceinline__ cx f_s1g30(const Pt &p0, const Pt &p1, const Pt &p2) {
-  const double d02 = p0.g - p2.g, d01 = p0.g - p1.g, d12 = p1.g - p2.g, t = d02 * d01;
-  cx v = cx(0.5 / d02, 0.0);
-  v = v - 0.5 / (t * t) * p0.Z * (-2.0 * p1.Z * p2.Z + p0.Z * (p1.Z + p2.Z)) * (p0.L - p1.L);
-  v = v + 0.5 / (d02 * d02) * p2.Z * p2.Z * (p1.L - p2.L) / d12;
-  return v + 0.5 / (d02 * d01) * p1.Z;
-}
-__device__ __forceinline__ cx f_s2g30g20(const Pt &p0, const Pt &p1) {
-  const double d = p0.g - p1.g;
-  return (d * (p0.Z + 2.0 * p1.Z) - 6.0 * p0.Z * p1.Z) / (12.0 * (d * d * d)) +
-         p0.Z * p1.Z * p1.Z * (p0.L - p1.L) / (d * d * d * d) * 0.5;
-}
-__device__ __forceinline__ cx f_s2g30g10(const Pt &p0, const Pt &p2) {
-  const double d = p0.g - p2.g;
-  return (2.0 * p0.Z * p0.Z - 7.0 * p0.Z * p2.Z + 11.0 * p2.Z * p2.Z) / (36.0 * (d * d * d)) -
-         p2.Z * p2.Z * p2.Z * (p0.L - p2.L) / (6.0 * (d * d * d * d));
-}
-__device__ __forceinline__ cx f_s2g10(const Pt &p0, const Pt &p2, const Pt &p3) {
-  const double d2 = p0.g - p2.g, d3 = p0.g - p3.g, d23 = p2.g - p3.g;
-  cx v = p0.Z * (p0.Z * p0.Z + 5.0 * p2.Z * p3.Z - 3.0 * p0.Z * (p2.Z + p3.Z)) / (12.0 * (d2 * d2) * (d3 * d3));
-  v = v - p2.Z * p2.Z * p2.Z * (p2.L - p0.L) / (6.0 * (d2 * d2 * d2) * d23);
-  return v + p3.Z * p3.Z * p3.Z * (p3.L - p0.L) / (6.0 * (d3 * d3 * d3) * d23);
-}
-__device__ __forceinline__ cx f_s2g30(const Pt &p0, const Pt &p1, const Pt &p2) {
-  const double d01 = p0.g - p1.g, d02 = p0.g - p2.g, d12 = p1.g - p2.g;
-  cx v = (p0.Z * p0.Z * d12 + p1.Z * p1.Z * d02) / (6.0 * d02 * (d01 * d01) * d12);
-  v = v - p0.Z * p0.Z * (2.0 * p1.Z * d02 + p2.Z * d01) * (p0.L - p2.L) / (6.0 * (d02 * d02) * (d01 * d01 * d01));
-  return v + p1.Z * p1.Z * (2.0 * p0.Z * d12 - p2.Z * d01) * (p1.L - p2.L) / (6.0 * (d01 * d01 * d01) * (d12 * d12));
-}
-
-// point at the average of the vertices in idx[0..n) (calc :243-296)
-__device__ __forceinline__ Pt avg_pt(const double (&g)[4], const int *idx, int n, double dg, cx w) {
-  double s = g[idx[0]];
-  for (int i = 1; i < n; i++) s += g[idx[i]];
-  Pt p;
-  p.g = s / (double)n;
-  p.Z = cx(p.g + w.r, dg + w.i);
-  p.L = clog_(p.Z);
-  return p;
-}
-
-// vertex terms of calc() for chk1 cases 2, 3 and 4 (one frequency, one sign),
-// positions 0..3; fk = dsgn on every vertex.  Returns false on a bad case.
-__device__ __forceinline__ bool degen_terms(const Chk &c, const Pt (&v)[4], const double (&g)[4], double dg, cx w,
-                                            double dsgn, cx (&x)[4]) {
-  switch (c.s) {
-  case 2: {
-    const Pt q = avg_pt(g, c.ia3, 2, dg, w);
-    const cx c1 = f_s2g10(q, v[c.ia4[0]], v[c.ia4[1]]);
-    const cx c2 = f_s2g30(q, v[c.ia4[0]], v[c.ia4[1]]);
-    const cx c3 = f_s1g30(q, v[c.ia4[1]], v[c.ia4[0]]);
-    x[c.ia3[0]] = c1 * dsgn;
-    x[c.ia3[1]] = c1 * dsgn;
-    x[c.ia4[0]] = c2 * dsgn;
-    x[c.ia4[1]] = (c3 - c2 - c1 - c1) * dsgn;
-    return true;
-  }
-  case 3: {
-    const Pt q = avg_pt(g, c.ia3, 3, dg, w);
-    const cx c1 = f_s2g30g10(q, v[c.ia4[0]]);
-    const cx c2 = f_s1g30g20(q, v[c.ia4[0]]);
-    x[c.ia3[0]] = c1 * dsgn;
-    x[c.ia3[1]] = c1 * dsgn;
-    x[c.ia3[2]] = c1 * dsgn;
-    x[c.ia4[0]] = (c2 - c1 - c1 - c1) * dsgn;
-    return true;
-  }
-  case 4:
-    if (c.i3 == 2) {
-      const Pt q1 = avg_pt(g, c.ia3, 2, dg, w), q2 = avg_pt(g, c.ia3 + 2, 2, dg, w);
-      const cx c1 = f_s2g30g20(q1, q2);
-      const cx c2 = f_s1g30g21(q1, q2);
-      x[c.ia3[0]] = c1 * dsgn;
-      x[c.ia3[1]] = c1 * dsgn;
-      x[c.ia3[2]] = (c2 - c1 - c1) * 0.5 * dsgn;
-      x[c.ia3[3]] = (c2 - c1 - c1) * 0.5 * dsgn;
-      return true;
-    } else if (c.i3 >= 3 && c.i3 <= 6) {
-      const double s4 = (g[c.ia3[0]] + g[c.ia3[1]] + g[c.ia3[2]] + g[c.ia3[3]]) / 4.0;
-      const cx c1 = 1.0 / (cx(s4 + w.r, dg + w.i) * 24.0);
-      for (int a = 0; a < 4; a++) x[c.ia3[a]] = c1 * dsgn;
-      return true;
-    }
-    return false;
-  default:
-    return false;
-  }
-}
-
 // Tetrahedron categories: the normal closed forms, the near-degenerate forms of
 // chk1's cases 2, 3, 4 (i3 = 2) and 4 (i3 = 3..6) on an uncut tetrahedron, and
 // the rest (cut by the Fermi level, or a case calc() does not know).
 enum { TC_NORMAL = 0, TC_S2, TC_S3, TC_S4A, TC_S4B, TC_OTHER, TC_NCAT, TC_SKIP = 255 };
 
-// One uncut near-degenerate (tetrahedron, sign) of category cat.  The forms are
-// those of degen_terms with every real difference of the tetrahedron turned
-// into a product of a few reciprocals once, outside the frequency loop: per
-// frequency only complex products and the averaged points' logs remain.
+// One uncut near-degenerate (tetrahedron, sign) of category cat: the reference's
+// special forms (sub1g30g21 ... sub2simple, m_tetrahedron_20170325.F:304-451)
+// at the averaged points of calc() (:243-296).  All points share the imaginary
+// part delt*dsgn, so every energy difference is real and log(z_a / z_b) =
+// L_a - L_b: vertex logs come from the shared table, only the averages need a
+// log of their own.  Every real difference of the tetrahedron is turned into a
+// product of a few reciprocals once, outside the frequency loop: per frequency
+// only complex products and the averaged points' logs remain.
 __device__ void degen_tetra(const TetraArgs &a, int code, int cat, const double *e1m, const double *e2m,
                             const double2 *Lt, int e0, int ne, int nec, double2 *xo) {
   const int t = code >> 1, sg = code & 1;
@@ -558,11 +458,12 @@ __device__ void degen_tetra(const TetraArgs &a, int code, int cat, const double 
   }
 }
 
-// One (tetrahedron, sign) that is near-degenerate or cut by the Fermi level:
-// ttct and the reference's closed forms (m_tetrahedron_20170325.F:99-302).
-// Out of line, so that its large local arrays do not weigh on the normal path.
-__device__ __noinline__ void other_tetra(const TetraArgs &a, int code, const double *e1m, const double *e2m,
-                                         const double2 *Lt, int e0, int ne, int nec, double2 *xo) {
+// One (tetrahedron, sign) that is cut by the Fermi level (or of a chk1 case
+// the other paths do not know): ttct and the reference's closed forms
+// (m_tetrahedron_20170325.F:99-302).  Out of line, so that its large local
+// arrays do not weigh on the other paths.
+__device__ __noinline__ void other_tetra(const TetraArgs &a, int code, const double *e1m, const double *e2m, int e0,
+                                         int ne, int nec, double2 *xo) {
   const double f = a.efermi, delt = a.delt;
   const int t = code >> 1, sg = code & 1;
   const double dsgn = sg == 0 ? 1.0 : -1.0;
@@ -573,34 +474,11 @@ __device__ __noinline__ void other_tetra(const TetraArgs &a, int code, const dou
   const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
   if (mn2 > f && mx1 < f) {
     cx ffk[4], ggk[4];
-    double g[4];
     for (int v = 0; v < 4; v++) {
       ffk[v] = cx(dsgn, 0);
       ggk[v] = cx(-(ee2[v] - ee1[v]), delt) * dsgn;
-      g[v] = ggk[v].r;
     }
-    const Chk c = chk1(a.dmna, a.dmnr, ggk);
-    const double dg = delt * dsgn;
-    for (int e = 0; e < ne; e++) {
-      const cx w(a.em[e0 + e].x, a.em[e0 + e].y);
-      cx x[4];
-      bool ok;
-      if (dg + w.i == 0.0) {
-        // z on the real axis: the reference's ratio logs
-        ok = calc_w(c, ffk, ggk, w, x);
-      } else {
-        Pt p[4];
-        for (int v = 0; v < 4; v++) {
-          p[v].g = g[v];
-          p[v].Z = ggk[v] + w;
-          const double2 l = Lt[((size_t)sg * a.ntk + slot[v]) * nec + e];
-          p[v].L = cx(l.x, l.y);
-        }
-        ok = degen_terms(c, p, g, dg, w, dsgn, x);
-      }
-      if (!ok) { atomicExch(a.err, 2); continue; }
-      for (int v = 0; v < 4; v++) sadd(&xo[slot[v] * nec + e], x[v]);
-    }
+    if (!tetra_terms(a.dmna, a.dmnr, ffk, ggk, a.em, e0, ne, nec, slot, nullptr, xo)) atomicExch(a.err, 2);
     return;
   }
   double dwgt[TT_NMAX][4][4], dvol[TT_NMAX];
@@ -752,7 +630,7 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
       degen_tetra(a, lists[idx], cat, e1m, e2m, Lt, e0, ne, nec, xo);
   // Fermi-cut tetrahedra and unknown cases: the reference's ttct and forms
   for (int idx = cbeg[TC_OTHER] + threadIdx.x; idx < cbeg[TC_OTHER + 1]; idx += blockDim.x)
-    other_tetra(a, lists[idx], e1m, e2m, Lt, e0, ne, nec, xo);
+    other_tetra(a, lists[idx], e1m, e2m, e0, ne, nec, xo);
   __syncthreads();
   // w[(p*nen + e)*ntk + k] = xow(mesh(k), e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
   for (int i = threadIdx.x; i < ntk * ne; i += blockDim.x) {
@@ -766,8 +644,217 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
   }
 }
 
-int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st) {
+// ---------------------------------------------------------------------------
+// Split-precision path: the FP32 series of rp_tetra_series.cuh for every
+// uncut tetrahedron where it converges, gathered per mesh vertex.
+//
+// Every tetrahedron is classified once, as the reference's calc() does (chk1:
+// normal, or near-degenerate with some vertices replaced by their average,
+// m_tetrahedron_20170325.F:209-302, 457-503), and its points' mean (FP64) and
+// deviations (FP32) go to shared memory.  Then one thread per (mesh slot,
+// frequency) walks the tetrahedra that touch the slot (24 on a cubic mesh) and
+// sums its vertex's weight over them and both signs in FP64 registers: no
+// atomics, one fixed summation order.  The weight is the
+// confluent divided difference of the tetrahedron's (averaged) points -- the
+// quantity the reference's closed forms (:304-451) evaluate -- and for each
+// (tetrahedron, sign, frequency) where the series does not converge (r > 1/2,
+// near resonance: the Lindhard denominators of near-degenerate band pairs)
+// the reference's closed forms run in FP64 instead.  Tetrahedra cut by the
+// Fermi level take ttct and the closed forms in FP64 (other_tetra) with
+// shared-memory sums; they exist only when a band is partially occupied.
+
+// A tetrahedron's code: its category in the low byte, then for each vertex
+// position (2 bits each) the position whose point it takes -- the first member
+// of its group of near-degenerate vertices, which share their average.
+__device__ __forceinline__ unsigned short tetra_code(int cat, const Chk &c) {
+  int rep[4] = {0, 1, 2, 3};
+  if (cat == TC_S2) {
+    rep[c.ia3[1]] = c.ia3[0];
+  } else if (cat == TC_S3) {
+    rep[c.ia3[1]] = c.ia3[0];
+    rep[c.ia3[2]] = c.ia3[0];
+  } else if (cat == TC_S4A) {
+    rep[c.ia3[1]] = c.ia3[0];
+    rep[c.ia3[3]] = c.ia3[2];
+  } else if (cat == TC_S4B) {
+    rep[c.ia3[1]] = rep[c.ia3[2]] = rep[c.ia3[3]] = c.ia3[0];
+  }
+  return (unsigned short)(cat | (rep[0] << 8) | (rep[1] << 10) | (rep[2] << 12) | (rep[3] << 14));
+}
+
+// the points of calc(): each vertex's value, or its group's average (:243-296)
+__device__ __forceinline__ void tetra_points(unsigned code, const double (&gr)[4], double (&gp)[4]) {
+  const double inv[5] = {0.0, 1.0, 0.5, 1.0 / 3.0, 0.25};
+#pragma unroll
+  for (int v = 0; v < 4; v++) {
+    const unsigned rv = (code >> (8 + 2 * v)) & 3u;
+    double s = 0.0;
+    int n = 0;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (((code >> (8 + 2 * u)) & 3u) == rv) { s += gr[u]; n++; }
+    gp[v] = n == 1 ? s : s * inv[n];
+  }
+}
+
+// vertex pos of tetrahedron t by the reference's closed forms for one sign
+// (fk = dsgn) at frequency w, FP64
+__device__ __noinline__ double2 closed_form_vertex(const TetraArgs &a, int t, const double *e1m, const double *e2m,
+                                                   double dsgn, double wr, double wi, int pos) {
+  cx ffk[4], ggk[4];
+  for (int v = 0; v < 4; v++) {
+    const int sl = a.imt1[4 * t + v];
+    ffk[v] = cx(dsgn, 0);
+    ggk[v] = cx(-(e2m[sl] - e1m[sl]), a.delt) * dsgn;
+  }
+  const Chk c = chk1(a.dmna, a.dmnr, ggk);
+  cx x[4];
+  if (!calc_w(c, ffk, ggk, cx(wr, wi), x)) {
+    atomicExch(a.err, 2);
+    return make_double2(0.0, 0.0);
+  }
+  const cx r = pos == 0 ? x[0] : pos == 1 ? x[1] : pos == 2 ? x[2] : x[3];
+  return make_double2(r.r, r.i);
+}
+
+// two CTAs per SM: the smem of a 512-k mesh allows two, and the register cap
+// leaves the hot gather loop unspilled
+__global__ void __launch_bounds__(256, 2) tetra_series_kernel(TetraArgs a, int nec, double2 *__restrict__ wout) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int p = blockIdx.x, e0 = blockIdx.y * nec, ntk = a.ntk;
+  const int ne = min(nec, a.nen - e0);
+  const int ntet = 6 * ntk;
+  // per tetrahedron: the FP32 deviations d of its points from their mean, the
+  // mean (FP64) and the code; per slot the pair's energies; for metals the
+  // sums of the cut tetrahedra and their list
+  float4 *td = (float4 *)smem;
+  double *tmean = (double *)(td + ntet);
+  double *e1m = tmean + ntet, *e2m = e1m + ntk;
+  double2 *xo = (double2 *)(e2m + ntk);
+  int *olist = (int *)(xo + (a.may_cut ? (size_t)ntk * nec : 0));
+  unsigned short *tcode = (unsigned short *)(olist + (a.may_cut ? 2 * (size_t)ntet : 0));
+  __shared__ int ncut;
+  const int bv = a.pair_vir[p], bo = a.pair_occ[p];
+  if (threadIdx.x == 0) ncut = 0;
+  for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
+    const int k = a.index_kpt[m];
+    e1m[m] = (double)(float)a.energy[(size_t)a.numirr[k] * a.ntb + bo];
+    e2m[m] = (double)(float)a.energy[(size_t)a.numirr[a.kpq[k]] * a.ntb + bv];
+  }
+  if (a.may_cut)
+    for (int i = threadIdx.x; i < ntk * nec; i += blockDim.x) xo[i] = make_double2(0, 0);
+  __syncthreads();
+  const double f = a.efermi, delt = a.delt;
+  // classify every tetrahedron (chk1 sees |g_a - g_b| and |g_a + g_b|, which the
+  // sign does not change, so one test covers both signs) and keep its points
+  for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
+    double ee1[4], ee2[4];
+    for (int v = 0; v < 4; v++) { const int sl = a.imt1[4 * t + v]; ee1[v] = e1m[sl]; ee2[v] = e2m[sl]; }
+    const double mn2 = fmin(fmin(ee2[0], ee2[1]), fmin(ee2[2], ee2[3]));
+    const double mx2 = fmax(fmax(ee2[0], ee2[1]), fmax(ee2[2], ee2[3]));
+    const double mx1 = fmax(fmax(ee1[0], ee1[1]), fmax(ee1[2], ee1[3]));
+    unsigned short code = TC_OTHER;
+    if (mx2 <= f) {
+      code = TC_SKIP;  // ttct(+1) drops the whole tetrahedron
+    } else if (mn2 > f && mx1 < f) {
+      cx ggk[4];
+      double gr[4];
+      for (int v = 0; v < 4; v++) {
+        gr[v] = -(ee2[v] - ee1[v]);
+        ggk[v] = cx(gr[v], delt);
+      }
+      const Chk c = chk1(a.dmna, a.dmnr, ggk);
+      const int cat = c.s == 0 ? TC_NORMAL : c.s == 2 ? TC_S2 : c.s == 3 ? TC_S3
+                    : c.s == 4 && c.i3 == 2 ? TC_S4A : c.s == 4 && c.i3 >= 3 && c.i3 <= 6 ? TC_S4B : TC_OTHER;
+      if (cat != TC_OTHER) {
+        code = tetra_code(cat, c);
+        double gp[4];
+        tetra_points(code, gr, gp);
+        const double mean = 0.25 * ((gp[0] + gp[1]) + (gp[2] + gp[3]));
+        tmean[t] = mean;
+        td[t] = make_float4((float)(gp[0] - mean), (float)(gp[1] - mean), (float)(gp[2] - mean), (float)(gp[3] - mean));
+      }
+    }
+    tcode[t] = code;
+    if (code == TC_OTHER) {
+      if (a.may_cut) {
+        const int o = atomicAdd(&ncut, 2);
+        olist[o] = 2 * t;
+        olist[o + 1] = 2 * t + 1;
+      } else {
+        atomicExch(a.err, 5);  // a cut tetrahedron although no band is partially occupied
+      }
+    }
+  }
+  __syncthreads();
+  if (a.may_cut) {
+    for (int idx = threadIdx.x; idx < ncut; idx += blockDim.x) other_tetra(a, olist[idx], e1m, e2m, e0, ne, nec, xo);
+    __syncthreads();
+  }
+  // one thread per (slot, frequency): the slot's vertex weight summed over the
+  // tetrahedra around it and both signs
+  for (int it = threadIdx.x; it < ntk * ne; it += blockDim.x) {
+    const int m = it % ntk, e = it / ntk;
+    const double2 w = a.em[e0 + e];
+    double ar = 0.0, ai = 0.0;
+    const int j1 = __ldg(a.inc_off + m + 1);
+    for (int j = __ldg(a.inc_off + m); j < j1; j++) {
+      const int ent = __ldg(a.inc + j), t = ent >> 2, pos = ent & 3;
+      const int cat = tcode[t] & 0xff;
+      if (cat == TC_SKIP || cat == TC_OTHER) continue;
+      const float4 d4 = td[t];
+      const float d[4] = {d4.x, d4.y, d4.z, d4.w};
+      const float dmax = fmaxf(fmaxf(fabsf(d4.x), fabsf(d4.y)), fmaxf(fabsf(d4.z), fabsf(d4.w)));
+      const float dv = pos == 0 ? d4.x : pos == 1 ? d4.y : pos == 2 ? d4.z : d4.w;
+      bool ok[2];
+      TsCplx x[2];
+      tetra_series_vertex2(d, dv, dmax, tmean[t], delt, w.x, w.y, ok, x);
+      // fk = dsgn: the sign -1 enters negated
+      ar += (double)x[0].r - (double)x[1].r;
+      ai += (double)x[0].i - (double)x[1].i;
+      if (!ok[0]) {
+        const double2 c = closed_form_vertex(a, t, e1m, e2m, 1.0, w.x, w.y, pos);
+        ar += c.x;
+        ai += c.y;
+      }
+      if (!ok[1]) {
+        const double2 c = closed_form_vertex(a, t, e1m, e2m, -1.0, w.x, w.y, pos);
+        ar += c.x;
+        ai += c.y;
+      }
+    }
+    // w[(p*nen + e)*ntk + k] = xow(m, e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
+    const int k = a.index_kpt[m];
+    const double2 po = a.prob[(size_t)k * a.ntb + bo], pv = a.prob[(size_t)a.kpq[k] * a.ntb + bv];
+    const double2 pp = make_double2(1.0 - (po.x * pv.x - po.y * pv.y), -(po.x * pv.y + po.y * pv.x));
+    double2 x = make_double2(ar, ai);
+    if (a.may_cut) x = cadd(x, xo[(size_t)m * nec + e]);
+    const double2 r = cmul(x, pp);
+    wout[((size_t)p * a.nen + e0 + e) * ntk + k] = make_double2(r.x / (double)ntk, r.y / (double)ntk);
+  }
+}
+
+int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st, bool series) {
   if (a.npair == 0) return 0;
+  if (series) {
+    if (!a.inc_off || !a.inc) fail(1, "tetrahedron series kernel: no vertex incidence lists");
+    // the tetrahedra's points and codes, e1m and e2m, plus for metals the
+    // cut-tetrahedron list and the sums of a frequency chunk
+    const size_t ntk = (size_t)a.ntk, ntet = 6 * ntk;
+    const size_t fixed = (sizeof(float4) + sizeof(double) + sizeof(unsigned short)) * ntet + 2 * sizeof(double) * ntk +
+                         (a.may_cut ? 2 * sizeof(int) * ntet : 0);
+    const size_t per_e = a.may_cut ? sizeof(double2) * ntk : 0;
+    int nec = a.nen;
+    while (nec > 1 && fixed + per_e * nec > 210 * 1024) nec--;
+    const size_t smem = fixed + per_e * nec;
+    if (smem > 227 * 1024) fail(1, "k mesh too large for the tetrahedron tile (%zu bytes)", smem);
+    RP_CUDA(cudaFuncSetAttribute(tetra_series_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_cap(tetra_series_kernel)));
+    dim3 grid(a.npair, (a.nen + nec - 1) / nec);
+    tetra_series_kernel<<<grid, 256, smem, st>>>(a, nec, w);
+    RP_CUDA(cudaGetLastError());
+    return 1;
+  }
   // weights (ntk x nec) and vertex logs (2 x ntk x nec) of a frequency chunk in shared memory
   int nec = a.nen;
   const size_t fixed = 2 * sizeof(double) * (size_t)a.ntk + 2 * 6 * sizeof(int) * (size_t)a.ntk + 6 * (size_t)a.ntk;

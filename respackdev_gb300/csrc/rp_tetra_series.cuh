@@ -98,4 +98,72 @@ RP_TS_HD bool tetra_series_weights(const double (&gr)[4], double dsgn, double de
   return true;
 }
 
+// a_n = (-1)^n n!/(n+4)! without its sign: 1 / ((n+1)(n+2)(n+3)(n+4))
+#define RP_TS_A(n) (1.0f / ((float)((n) + 1) * (float)((n) + 2) * (float)((n) + 3) * (float)((n) + 4)))
+#define RP_TS_A5(n) RP_TS_A(n), RP_TS_A(n + 1), RP_TS_A(n + 2), RP_TS_A(n + 3), RP_TS_A(n + 4)
+#if defined(__CUDA_ARCH__)
+static __constant__ float kTsA[TS_NMAX] = {RP_TS_A5(0), RP_TS_A5(5), RP_TS_A5(10), RP_TS_A5(15), RP_TS_A5(20),
+                                           RP_TS_A5(25)};
+#else
+static const float kTsA[TS_NMAX] = {RP_TS_A5(0), RP_TS_A5(5), RP_TS_A5(10), RP_TS_A5(15), RP_TS_A5(20),
+                                    RP_TS_A5(25)};
+#endif
+
+// The weight of one vertex for both signs at once.  d[i] = g_i - gbar (FP32)
+// for the sign +1, with g_i the tetrahedron's points (near-degenerate vertices
+// already replaced by their average, as the reference's calc() does) and gbar
+// = mean their mean (double); dv = d of the vertex; dmax = max |d|.  The sign
+// -1 negates every d, so it shares the h_n and its terms carry (-1)^n; its z
+// is w - gbar - i delt.  ok[s] says whether the series was taken for sign s
+// (s = 0: +1, s = 1: -1): false where r > TS_RMAX or z = 0, x[s] then 0.
+// Values in the closed forms' normalisation (before the factor fk = dsgn).
+RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, double mean, double delt, double wr,
+                                   double wi, bool (&ok)[2], TsCplx (&x)[2]) {
+  float ur[2], ui[2], rmax = 0.f;
+  for (int s = 0; s < 2; s++) {
+    const double sg = s == 0 ? 1.0 : -1.0;
+    // z in double (one subtraction's worth of care), the rest in FP32
+    const float zr = (float)(wr + sg * mean), zi = (float)(wi + sg * delt);
+    const float zz = zr * zr + zi * zi;
+    ok[s] = zz > 0.f && dmax * dmax <= TS_RMAX * TS_RMAX * zz;
+    const float inv = ok[s] ? 1.f / zz : 0.f;
+    ur[s] = zr * inv;
+    ui[s] = -zi * inv;
+    if (ok[s]) rmax = fmaxf(rmax, dmax * sqrtf(inv));
+    x[s] = TsCplx{0.f, 0.f};
+  }
+  if (!ok[0] && !ok[1]) return;
+  // n = 0: a_0 u
+  float pr0 = ur[0], pi0 = ui[0], pr1 = ur[1], pi1 = ui[1];
+  float sr0 = kTsA[0] * pr0, si0 = kTsA[0] * pi0, sr1 = kTsA[0] * pr1, si1 = kTsA[0] * pi1;
+  float h1 = 1.f, h2 = 1.f, h3 = 1.f, h4 = 1.f, hv = 1.f;
+  // term n is at most r^n times the first: take terms while r^(n-1) > 2^-24
+  float rprev = 1.f;
+  float sgn = 1.f;
+  for (int n = 1; n < TS_NMAX && rprev > 5.9604645e-8f; n++) {
+    h1 = d[0] * h1;
+    h2 = h1 + d[1] * h2;
+    h3 = h2 + d[2] * h3;
+    h4 = h3 + d[3] * h4;
+    hv = h4 + dv * hv;
+    sgn = -sgn;
+    const float t = sgn * kTsA[n] * hv;
+    float q = pr0 * ur[0] - pi0 * ui[0];
+    pi0 = pr0 * ui[0] + pi0 * ur[0];
+    pr0 = q;
+    sr0 += t * pr0;
+    si0 += t * pi0;
+    q = pr1 * ur[1] - pi1 * ui[1];
+    pi1 = pr1 * ui[1] + pi1 * ur[1];
+    pr1 = q;
+    // sign -1: its d are negated, so its h_n carry (-1)^n
+    const float t1 = (n & 1) ? -t : t;
+    sr1 += t1 * pr1;
+    si1 += t1 * pi1;
+    rprev *= rmax;
+  }
+  if (ok[0]) x[0] = TsCplx{sr0, si0};
+  if (ok[1]) x[1] = TsCplx{sr1, si1};
+}
+
 }  // namespace rp

@@ -88,8 +88,9 @@ def test_mixed_inverse_matches_fp64_inverse(headline):
         for iq in QS:
             c1 = mixed.chi0_q(iq)
             c2 = full.chi0_q(iq)
-            # same inputs, same kernels: identical chi, so only the inversion differs
-            assert np.array_equal(c1, c2)
+            # same inputs, same kernels: chi equal up to the order of floating-point
+            # sums, so the difference below is the inversion's
+            assert normwise_err(c1, c2) < 1e-12
             e1 = mixed.epsinv_q()
             e2 = full.epsinv_q()
             worst = max(worst, normwise_err(e1, e2))

@@ -115,3 +115,70 @@ def test_series_weights_match_the_closed_forms(tmp_path):
     assert worst < 1e-6
     assert ok_eq == 1 and eqerr < 1e-6
     assert took_res == 0
+
+
+HARNESS2 = r"""
+#include <cmath>
+#include <cstdio>
+#include <random>
+#include "rp_tetra_series.cuh"
+// tetra_series_vertex2 (one vertex, both signs, the kernel's form) against
+// tetra_series_weights (all four vertices, one sign) on random points
+int main() {
+  std::mt19937_64 rng(777);
+  std::uniform_real_distribution<double> U(0.0, 1.0);
+  const double delt = 0.01;
+  long n = 0, n_ok = 0, n_mismatch_flag = 0;
+  double worst = 0;
+  for (int it = 0; it < 100000; it++) {
+    double gr[4];
+    const double c = -1.5 + 3.0 * U(rng), s = std::exp(std::log(1e-4) + (std::log(0.1) - std::log(1e-4)) * U(rng));
+    for (int v = 0; v < 4; v++) gr[v] = c + s * (2.0 * U(rng) - 1.0);
+    if (U(rng) < 0.2) gr[1] = gr[0];                 // averaged (degenerate) points
+    if (U(rng) < 0.1) gr[3] = gr[2] = gr[0];
+    const bool imag = U(rng) < 0.5;
+    const double wm = 1.5 * U(rng), wr = imag ? 0.0 : wm, wi = imag ? wm : 0.0;
+    const double mean = 0.25 * ((gr[0] + gr[1]) + (gr[2] + gr[3]));
+    float d[4], dmax = 0.f;
+    for (int v = 0; v < 4; v++) { d[v] = (float)(gr[v] - mean); dmax = std::fmax(dmax, std::fabs(d[v])); }
+    for (int pos = 0; pos < 4; pos++) {
+      bool ok[2];
+      rp::TsCplx x2[2];
+      rp::tetra_series_vertex2(d, d[pos], dmax, mean, delt, wr, wi, ok, x2);
+      for (int sgi = 0; sgi < 2; sgi++) {
+        rp::TsCplx x4[4];
+        const bool ok4 = rp::tetra_series_weights(gr, sgi == 0 ? 1.0 : -1.0, delt, wr, wi, x4);
+        n++;
+        if (ok4 != ok[sgi]) { n_mismatch_flag++; continue; }
+        if (!ok4) continue;
+        n_ok++;
+        const double den = std::hypot(x4[pos].r, x4[pos].i);
+        const double e = std::hypot(x2[sgi].r - x4[pos].r, x2[sgi].i - x4[pos].i) / den;
+        if (e > worst) worst = e;
+      }
+    }
+  }
+  std::printf("%ld %ld %ld %.3e\n", n, n_ok, n_mismatch_flag, worst);
+  return 0;
+}
+"""
+
+
+def test_vertex_series_both_signs_matches_four_vertex_form(tmp_path):
+    """The kernel's form (one vertex, both signs sharing the h_n recurrence, the
+    sign -1 through (-1)^n) equals the four-vertex form per sign to FP32
+    rounding, and declines the same (tetrahedron, sign, frequency) cases."""
+    src = tmp_path / "h2.cpp"
+    exe = tmp_path / "h2"
+    src.write_text(HARNESS2)
+    r = subprocess.run(["g++", "-O2", "-std=c++17", f"-I{ROOT}/respackdev_gb300/csrc", str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.fail(r.stderr)
+    n, n_ok, n_flag, worst = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    n, n_ok, n_flag, worst = int(n), int(n_ok), int(n_flag), float(worst)
+    print(f"{n_ok}/{n} on the series, {n_flag} decided differently, worst difference {worst:.2e}")
+    # the r <= 1/2 test is the same up to rounding at the boundary
+    assert n_flag < 1e-4 * n
+    assert n_ok > 0.5 * n
+    assert worst < 2e-6
