@@ -73,6 +73,11 @@ typedef struct rp_params {
                                   the FP64 Gauss-Jordan (0: FP32 Gauss-Jordan
                                   plus one float-pair Newton step, FP64 only
                                   as its fallback)                            */
+  char   tail_model[256];      /* band-tail network file (written by
+                                  respackdev_gb300.tail.TailMLP.save); when set,
+                                  rp_chi0_q adds the network's prediction of
+                                  the bands above N_CALC_BAND to the diagonal
+                                  of chi0.  Empty: no correction.             */
 } rp_params;
 
 /* Defaults of m_rdinput.f90:52-73 (Num_freq_grid=70, Green_func_delt=0.1 eV, ...). */
@@ -150,6 +155,16 @@ void rp_reset_tuner(void);
  * invZGE (chiqw_sub.F:386-568, invZGE.F90:1-22), FP64 on the device.
  * Layout as chi.  epsinv may be NULL. */
 int rp_epsinv_q(rp_ctx *ctx, double *epsinv);
+
+/* eps^-1 of the q point of the last rp_chi0_q from a chi0 the caller supplies
+ * in rp_chi0_q's layout (for instance a chi0 the caller corrected): the device
+ * chi0 of that q is replaced by chi, then rp_epsinv_q runs.  No reference
+ * counterpart (the reference inverts only its own chi, chiqw.F:1515-1525). */
+int rp_epsinv_chi_q(rp_ctx *ctx, const double *chi, double *epsinv);
+
+/* 1 if the last rp_chi0_q added the band-tail network's correction (a context
+ * created with tail_model), else 0. */
+int rp_tail_applied(const rp_ctx *ctx);
 
 /* Write dir-eps/qNNN for the last rp_chi0_q/rp_epsinv_q: dat.sq,
  * dat.epsqw.600(-602), dat.epsqw.6NN0MM text diagonals and dat.log.400 last

@@ -36,6 +36,7 @@ class Params(C.Structure):
         ("dump_chi", C.c_int), ("device", C.c_int), ("max_pairs", C.c_int), ("qshard_index", C.c_int),
         ("qshard_count", C.c_int), ("pair_fp64", C.c_int), ("tc_ksub", C.c_int),
         ("pair_batch", C.c_int), ("tc_split", C.c_int), ("write_eps_f32", C.c_int), ("eps_fp64", C.c_int),
+        ("tail_model", C.c_char * 256),
     ]
 
 
@@ -72,6 +73,10 @@ def load() -> C.CDLL:
     L.rp_chi0_q.restype = C.c_int
     L.rp_epsinv_q.argtypes = [vp, vp]
     L.rp_epsinv_q.restype = C.c_int
+    L.rp_epsinv_chi_q.argtypes = [vp, vp, vp]
+    L.rp_epsinv_chi_q.restype = C.c_int
+    L.rp_tail_applied.argtypes = [vp]
+    L.rp_tail_applied.restype = C.c_int
     L.rp_write_q.argtypes = [vp, C.c_char_p]
     L.rp_write_q.restype = C.c_int
     L.rp_calc_chiqw.argtypes = [C.c_char_p, C.c_char_p]
@@ -104,6 +109,8 @@ def default_params(**kw) -> Params:
     for k, v in kw.items():
         if k == "fft_box":
             p.fft_box[0], p.fft_box[1], p.fft_box[2] = v
+        elif k == "tail_model":
+            p.tail_model = v.encode() if isinstance(v, str) else v
         else:
             setattr(p, k, v)
     return p
@@ -182,6 +189,26 @@ class Context:
         out = np.empty(self.ndir * nen * self.ng * self.ng, dtype=np.complex128)
         self._check(self.L.rp_epsinv_q(self._h, out.ctypes.data), "rp_epsinv_q")
         return out.reshape(self.ndir, nen, self.ng, self.ng).transpose(3, 2, 1, 0)
+
+    def epsinv_chi_q(self, chi: np.ndarray, fetch: bool = True) -> Optional[np.ndarray]:
+        """eps^-1 of the last chi0_q's q point from a caller chi0 shaped like chi0_q's."""
+        nen = self.info().nen
+        a = np.asarray(chi, dtype=np.complex128)
+        if a.ndim == 3:
+            a = a[..., None]
+        if a.shape != (self.ng, self.ng, nen, self.ndir):
+            raise ValueError(f"chi0 must be {(self.ng, self.ng, nen, self.ndir)}, got {a.shape}")
+        buf = np.ascontiguousarray(a.transpose(3, 2, 1, 0))
+        out = np.empty(self.ndir * nen * self.ng * self.ng, dtype=np.complex128) if fetch else None
+        self._check(self.L.rp_epsinv_chi_q(self._h, buf.ctypes.data, out.ctypes.data if fetch else None),
+                    "rp_epsinv_chi_q")
+        if not fetch:
+            return None
+        return out.reshape(self.ndir, nen, self.ng, self.ng).transpose(3, 2, 1, 0)
+
+    def tail_applied(self) -> bool:
+        """True if the last chi0_q added the band-tail network's correction."""
+        return bool(self.L.rp_tail_applied(self._h))
 
     def write_q(self, root: Optional[str] = None):
         self._check(self.L.rp_write_q(self._h, (root or self.root).encode()), "rp_write_q")

@@ -74,6 +74,14 @@ struct rp_ctx {
   DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
       rowcol, A, eps, prow, fcol, piv, used, intra, pwpl, mixws, mixaux;
   rp::TcWorkspace tcw;
+  // band-tail network (&param_gpu tail_model): the network, its shell count and
+  // target scale, the excluded-band statistics, and the per-q shell map,
+  // features and whether the last rp_chi0_q applied it
+  rp_mlp *tail = nullptr;
+  int tail_nshell = 0;
+  float tail_scale = 1.f, tail_stats[3]{};
+  DevBuf tail_sh, tail_x;
+  bool tail_done = false;
   rp::QTask task;
   int ndir = 1;
   double wd[3]{};
@@ -90,9 +98,10 @@ struct rp_ctx {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &inc_off, &inc, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
                       &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
-                      &intra, &pwpl, &mixws, &mixaux})
+                      &intra, &pwpl, &mixws, &mixaux, &tail_sh, &tail_x})
       b->release();
     tcw.release();
+    if (tail) rp_mlp_destroy(tail);
     for (auto &e : ev) if (e) cudaEventDestroy(e);
     for (auto &e : sev) if (e) cudaEventDestroy(e);
     if (stage) cudaFreeHost(stage);
@@ -134,6 +143,77 @@ static void check_device_error(rp_ctx *c) {
   if (e == 3) rp::fail(-3, "dielectric matrix is singular");
   if (e == 4) rp::fail(-3, "tensor-core contraction: wait limit reached");
   if (e == 5) rp::fail(-3, "a tetrahedron is cut by the Fermi level although no band is partially occupied");
+}
+
+// The band-tail network file written by respackdev_gb300.tail.TailMLP.save:
+// int32 magic "RPTL", version 1, nin, nhid, nout, nshell; float32 target scale,
+// one float32 of padding; then the nparams float32 parameters in rp_mlp's order.
+static void load_tail(rp_ctx *c, const std::string &path) {
+  FILE *f = fopen(path.c_str(), "rb");
+  if (!f) rp::fail(1, "cannot open the band-tail network %s", path.c_str());
+  int32_t h[6];
+  float sc[2];
+  const bool ok = fread(h, 4, 6, f) == 6 && fread(sc, 4, 2, f) == 2;
+  if (!ok || h[0] != 0x4c545052 || h[1] != 1) { fclose(f); rp::fail(1, "%s is not a band-tail network file", path.c_str()); }
+  if (h[2] != 9 || h[4] != 2 || h[5] < 1 || h[5] > 256 || !(sc[0] > 0.f)) {
+    fclose(f);
+    rp::fail(1, "%s: a band-tail network takes 9 features and gives 2 outputs per shell", path.c_str());
+  }
+  rp_mlp *m = nullptr;
+  int rc = rp_mlp_create(&m, h[2], h[3], h[4], 0, c->dev);
+  if (rc) { fclose(f); rp::fail(rc, "band-tail network: %s", rp_last_error(nullptr)); }
+  std::vector<float> prm((size_t)rp_mlp_nparams(m));
+  if (fread(prm.data(), 4, prm.size(), f) != prm.size()) {
+    fclose(f);
+    rp_mlp_destroy(m);
+    rp::fail(1, "%s: short parameter block", path.c_str());
+  }
+  fclose(f);
+  rc = rp_mlp_set_params(m, prm.data());
+  if (rc) { rp_mlp_destroy(m); rp::fail(rc, "band-tail network: cannot upload its parameters"); }
+  c->tail = m;
+  c->tail_nshell = h[5];
+  c->tail_scale = sc[0];
+  // the excluded bands (N_CALC_BAND+1 .. NTB) over the listed k points, as tail.band_stats
+  const rp::Setup &S = c->S;
+  if (S.ncb >= S.ntb) rp::fail(1, "tail_model needs N_CALC_BAND below the number of bands (%d)", S.ntb);
+  double lo = 1e300, sum = 0.0;
+  long n = 0;
+  for (int ib = S.ncb; ib < S.ntb; ib++)
+    for (int ik = 0; ik < S.nk_irr; ik++) {
+      const double e = S.e_eigi[(size_t)ik * S.ntb + ib] - S.efermi;
+      lo = std::min(lo, e);
+      sum += e;
+      n++;
+    }
+  c->tail_stats[0] = (float)lo;
+  c->tail_stats[1] = (float)(sum / (double)n);
+  c->tail_stats[2] = (float)((double)(S.ntb - S.ncb) / (double)std::max(S.ncb, 1));
+}
+
+// Shells of the G of a q (equal-count quantiles of |q+G| > 0, -1 for the head)
+// and the network's correction of the diagonal of chi0 (rp_tail.cu).
+static void tail_apply(rp_ctx *c, const rp::QTask &t, DevBuf &chi, int nen, int ndir) {
+  c->tail_done = false;
+  if (!c->tail) return;
+  const int ng = t.ng, ns = c->tail_nshell;
+  std::vector<int> ok, sh(ng, -1);
+  for (int g = 0; g < ng; g++)
+    if (t.qglen[g] > 0) ok.push_back(g);
+  std::stable_sort(ok.begin(), ok.end(), [&](int a, int b) { return t.qglen[a] < t.qglen[b]; });
+  const long n = (long)ok.size();
+  for (long i = 0; i < n; i++) sh[ok[i]] = (int)std::min<long>((i * ns) / std::max<long>(n, 1), ns - 1);
+  cudaStream_t st = c->st;
+  upload(c->tail_sh, sh, st);
+  upload(c->qglen, t.qglen, st);  // another q of this context may have replaced it (ragged batches)
+  c->tail_x.ensure(sizeof(float) * (size_t)nen * ns * 9);
+  c->launches += rp::launch_tail_features(chi.as<double2>(), ng, nen, c->tail_sh.as<int>(), c->qglen.as<double>(), ns,
+                                          c->em.as<double2>(), c->tail_stats, c->tail_x.as<float>(), st);
+  const float *y = rp::mlp_forward_device(c->tail, c->tail_x.as<float>(), nen * ns, st);
+  c->launches += 3;
+  c->launches += rp::launch_tail_apply(chi.as<double2>(), ng, nen, ndir, c->tail_sh.as<int>(), c->qglen.as<double>(),
+                                       ns, y, c->tail_scale, st);
+  c->tail_done = true;
 }
 
 static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const double *em, int nen_explicit) {
@@ -196,6 +276,14 @@ static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const do
                                           c->kg0.as<int>(), S.ntk, S.ncb, S.ntg, S.nw[0], S.nw[1], S.nw[2], c->R[0],
                                           c->R[1], c->R[2], c->cfull.as<double2>(), c->ur.as<float2>(), 0, S.ntk, st);
   RP_CUDA(cudaStreamSynchronize(st));
+  if (p->tail_model[0]) {
+    char path[sizeof p->tail_model + 1];
+    std::memcpy(path, p->tail_model, sizeof p->tail_model);
+    path[sizeof p->tail_model] = 0;
+    std::string tp(path);
+    if (tp[0] != '/') tp = c->root + "/" + tp;  // relative to the run directory
+    load_tail(c, tp);
+  }
 }
 
 // Band pairs of one batch grouped by virtual band into chunks of <= jmax.
@@ -471,6 +559,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   for (int bi = 0; bi < q_nbatch(r); bi++) q_batch(c, r, bi, &c->tcw, true);
   if (fast) c->launches += rp::tc_end_q(c->tcw, c->chi.as<double2>(), nullptr, c->st);
   q_end(c, r);
+  tail_apply(c, c->task, c->chi, r.nen, r.ndir);
   float tot = 0;
   RP_CUDA(cudaEventElapsedTime(&tot, c->ev[5], c->ev[4]));
   c->times[0] = r.tms[0] * 1e-3; c->times[1] = r.tms[1] * 1e-3; c->times[2] = r.tms[2] * 1e-3;
@@ -788,6 +877,7 @@ int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, dou
     for (int i = 0; i < n; i++) {
       Prob &p = *P[i];
       q_end(p.c, p.r);
+      tail_apply(p.c, p.task, p.chi, p.r.nen, p.r.ndir);
       if (ng_out) ng_out[i] = p.r.ng;
       if (ndir_out) ndir_out[i] = p.r.ndir;
       if (chi && chi[i]) fetch_to(p.c, p.chi.p, chi[i], sizeof(cd) * (size_t)p.r.ndir * p.r.nen * p.r.ng * p.r.ng);
@@ -814,6 +904,22 @@ int rp_epsinv_q(rp_ctx *c, double *epsinv) {
     }
   });
 }
+
+int rp_epsinv_chi_q(rp_ctx *c, const double *chi, double *epsinv) {
+  if (!c) return 1;
+  return guarded(c, [&] {
+    if (!c->have_chi) rp::fail(1, "rp_epsinv_chi_q needs a preceding rp_chi0_q (its q point)");
+    if (!chi) rp::fail(1, "rp_epsinv_chi_q: chi is NULL");
+    RP_CUDA(cudaSetDevice(c->dev));
+    const size_t bytes = sizeof(cd) * result_elems(c);
+    RP_CUDA(cudaMemcpyAsync(c->chi.p, chi, bytes, cudaMemcpyHostToDevice, c->st));
+    t_h2d += (long long)bytes;
+    epsinv_run(c);
+    if (epsinv) fetch_to(c, c->eps.p, epsinv, bytes);
+  });
+}
+
+int rp_tail_applied(const rp_ctx *c) { return c && c->tail_done ? 1 : 0; }
 
 int rp_write_q(rp_ctx *c, const char *root) {
   if (!c) return 1;

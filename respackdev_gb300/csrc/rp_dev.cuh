@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/respack_gb300.h"
+
 namespace rp {
 
 // ---- complex arithmetic on float2/double2 (device code only) ----------------
@@ -163,5 +165,17 @@ size_t epsinv_mixed_bytes(int n, int nmat);
 int launch_epsinv_mixed(const double2 *A, int n, int nmat, void *ws, int *piv, int *used, double2 *out,
                         float *rnorm, int *err, cudaStream_t st);
 int launch_scale(double2 *x, size_t n, double divisor, cudaStream_t st);  // x /= divisor
+
+// band-tail correction (rp_tail.cu): X[(e*nshell + s)*9 + j] features of shell s
+// at frequency e from the diagonal of chi (direction 0); sh[g] = shell of G (-1:
+// none); stats = {lowest, mean excluded band energy above E_F, excluded/included}
+int launch_tail_features(const double2 *chi, int ng, int nen, const int *sh, const double *qglen, int nshell,
+                         const double2 *em, const float *stats, float *X, cudaStream_t st);
+// chi(G,G,w) += Y[(e*nshell + sh[G])*2 + {0,1}] / tscale |q+G|^2 / (4 pi), every direction
+int launch_tail_apply(double2 *chi, int ng, int nen, int ndir, const int *sh, const double *qglen, int nshell,
+                      const float *Y, float tscale, cudaStream_t st);
+// the network's forward pass on device inputs X (B x nin) on stream st; returns
+// the device outputs (B x nout), valid until the network's next call
+const float *mlp_forward_device(rp_mlp *m, const float *X, int B, cudaStream_t st);
 
 }  // namespace rp

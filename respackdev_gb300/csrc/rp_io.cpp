@@ -290,6 +290,13 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "tc_split") p->tc_split = nl_int(v, k);
       else if (k == "write_eps_f32") p->write_eps_f32 = nl_int(v, k);
       else if (k == "eps_fp64") p->eps_fp64 = nl_int(v, k);
+      else if (k == "tail_model") {
+        const std::string path = v.empty() ? "" : v[0];
+        if (path.size() >= sizeof p->tail_model) fail(1, "&param_gpu tail_model: path longer than %zu characters",
+                                                      sizeof p->tail_model - 1);
+        std::memset(p->tail_model, 0, sizeof p->tail_model);
+        std::memcpy(p->tail_model, path.data(), path.size());
+      }
       else if (k == "freq_re_ev") for (auto &x : v) fre.push_back(to_num(x));
       else if (k == "freq_im_ev") for (auto &x : v) fim.push_back(to_num(x));
       else fail(1, "namelist &param_gpu: unknown name '%s'", k.c_str());

@@ -158,18 +158,20 @@ Act acts(rp_mlp *m, int B) {
   return a;
 }
 
-// forward on device inputs X (B x nin); leaves the activations in m->act
-void forward(rp_mlp *m, const float *X, int B) {
+// forward on device inputs X (B x nin) on stream st (default: the network's
+// own); leaves the activations in m->act
+void forward(rp_mlp *m, const float *X, int B, cudaStream_t st = nullptr) {
+  if (!st) st = m->st;
   ensure_act(m, B);
   Act a = acts(m, B);
   const unsigned nb = (unsigned)((B + 31) / 32);
   const __nv_bfloat16 *pb = m->pb;
-  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nin, m->st>>>(X, B, m->nin, pb + m->oW1, pb + m->ob1, m->nhid,
-                                                                    1, a.Z1, a.H1);
-  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nhid, m->st>>>(a.H1, B, m->nhid, pb + m->oW2, pb + m->ob2,
-                                                                     m->nhid, 1, a.Z2, a.H2);
-  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nhid, m->st>>>(a.H2, B, m->nhid, pb + m->oW3, pb + m->ob3,
-                                                                     m->nout, 0, nullptr, a.Y);
+  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nin, st>>>(X, B, m->nin, pb + m->oW1, pb + m->ob1, m->nhid, 1,
+                                                                  a.Z1, a.H1);
+  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nhid, st>>>(a.H1, B, m->nhid, pb + m->oW2, pb + m->ob2,
+                                                                   m->nhid, 1, a.Z2, a.H2);
+  rp::mlp_dense_fwd<<<nb, 256, sizeof(float) * 32 * m->nhid, st>>>(a.H2, B, m->nhid, pb + m->oW3, pb + m->ob3,
+                                                                   m->nout, 0, nullptr, a.Y);
   RP_CUDA(cudaGetLastError());
 }
 
@@ -194,6 +196,17 @@ void backward(rp_mlp *m, const float *X, const float *T, int B) {
   rp::mlp_dense_bwd_w<<<m->nhid, 128, 0, m->st>>>(a.dH1, X, B, m->nhid, m->nin, m->g + m->oW1, m->g + m->ob1);
   RP_CUDA(cudaGetLastError());
 }
+
+}  // namespace
+
+const float *rp::mlp_forward_device(rp_mlp *m, const float *X, int B, cudaStream_t st) {
+  // the network's own stream may still be finishing a set_params upload
+  RP_CUDA(cudaStreamSynchronize(m->st));
+  forward(m, X, B, st);
+  return acts(m, B).Y;
+}
+
+namespace {
 
 template <typename F>
 int guarded(rp_mlp *m, F &&f) {

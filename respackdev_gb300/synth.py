@@ -57,6 +57,12 @@ class SynthSpec:
     wan_mode: str = "identity"    # identity | random  (dat.umat)
     nwf: int = 0                  # Wannier orbitals for calc_int (0 = none)
     wan_sigma: float = 1.2        # Gaussian width of the synthetic orbitals (bohr)
+    # symmetry written to dat.symmetry: "identity" (the whole mesh in
+    # dat.sample-k), "oh" (the 48 point operations of the cubic lattice, an
+    # irreducible dat.sample-k) or "oh_glide" (as "oh", with the fractional
+    # translation (1/4, 1/4, 1/4) of the diamond structure on the 24
+    # operations outside T_d: nnp = 4)
+    sym: str = "identity"
 
 
 # ----------------------------------------------------------------------------
@@ -211,19 +217,110 @@ class SynthData:
     avec: np.ndarray
     bvec: np.ndarray
     volume: float
-    kpts: np.ndarray           # (nk, 3) fractional
+    kpts: np.ndarray           # (nk, 3) fractional (the irreducible list with symmetry)
     kg: List[np.ndarray]       # per k: (npw_k, 3) int
     coeffs: List[np.ndarray]   # per k: (npw_k, nbands) complex
     energies: np.ndarray       # (nbands, nk) Hartree
     efermi: float              # Hartree
     ecut_psi: float            # Ry
+    # dat.symmetry: rotations on fractional reciprocal coordinates (k' = rg k,
+    # identity first), fractional translations pg / nnp
+    rg: List[np.ndarray] = dataclasses.field(default_factory=lambda: [np.eye(3, dtype=np.int64)])
+    pg: List[np.ndarray] = dataclasses.field(default_factory=lambda: [np.zeros(3, dtype=np.int64)])
+    nnp: int = 1
+
+
+def cubic_point_group(bvec: np.ndarray, glide: bool = False):
+    """The 48 operations of O_h on fractional reciprocal coordinates (the
+    reference's SK0 = rg SKI, chiqw.F:437-480), identity first: for each signed
+    permutation R (Cartesian) rg = B^-T R B^T, an integer matrix for the fcc,
+    bcc and simple-cubic lattices.  With glide, the operations outside T_d
+    (sign product -1) carry the translation (1/4, 1/4, 1/4) of the primitive
+    vectors (pg = (1, 1, 1), nnp = 4)."""
+    import itertools
+    BT = bvec.T
+    BTinv = np.linalg.inv(BT)
+    ops = []
+    for perm in itertools.permutations(range(3)):
+        for signs in itertools.product((1, -1), repeat=3):
+            R = np.zeros((3, 3))
+            for i in range(3):
+                R[i, perm[i]] = signs[i]
+            rg = BTinv @ R @ BT
+            rgi = np.rint(rg).astype(np.int64)
+            if not np.allclose(rg, rgi, atol=1e-9):
+                raise ValueError("the lattice does not have the cubic point group")
+            tau = np.ones(3, dtype=np.int64) if (glide and signs[0] * signs[1] * signs[2] < 0) else np.zeros(3, np.int64)
+            ident = perm == (0, 1, 2) and signs == (1, 1, 1)
+            ops.append((0 if ident else 1, rgi, tau))
+    ops.sort(key=lambda o: o[0])
+    return [o[1] for o in ops], [o[2] for o in ops], (4 if glide else 1)
+
+
+def _kmatch(a: np.ndarray, b: np.ndarray) -> bool:
+    return bool(np.all(np.abs(a - b) < 1.0e-4))
+
+
+def unfold_plan(kirr: np.ndarray, rg: List[np.ndarray]):
+    """The full mesh the reference builds from an irreducible list
+    (chiqw.F:437-480): per irreducible k and operation the image R k folded by
+    kcheck, then its time-reversed image folded by kcheck_trs, each kept when
+    new.  Returns [(SK0, numirr, numrot, trs, RW)] in that order (0-based)."""
+    out = []
+    for ik in range(kirr.shape[0]):
+        for iop, R in enumerate(rg):
+            kt, RW = _kcheck(R @ kirr[ik], False)
+            if not any(_kmatch(o[0], kt) for o in out):
+                out.append((kt, ik, iop, 1, RW))
+            kt, RW = _kcheck(R @ kirr[ik], True)
+            if not any(_kmatch(o[0], -kt) for o in out):
+                out.append((-kt, ik, iop, -1, RW))
+    return out
+
+
+def irreducible_mesh(nk: Sequence[int], rg: List[np.ndarray]) -> np.ndarray:
+    """Irreducible points of the Gamma-centred mesh under rg and time reversal,
+    the first of each star in mesh order, such that unfold_plan covers the mesh."""
+    mesh = gamma_mesh(nk)
+    kept: List[np.ndarray] = []
+    covered: List[np.ndarray] = []
+    for k in mesh:
+        if any(_kmatch(c, k) for c in covered):
+            continue
+        kept.append(k)
+        covered = [o[0] for o in unfold_plan(np.array(kept), rg)]
+    if len(covered) != mesh.shape[0]:
+        raise ValueError("the operations do not map the mesh onto itself")
+    return np.array(kept)
+
+
+def _check_cutoff(bvec: np.ndarray, ecut: float, kpts: np.ndarray):
+    """No |k+G|^2 within 1e-9 (relative) of the cutoff, so that every reader's
+    sphere (numpy here, C in the library and the oracle) holds the same G."""
+    for k in kpts:
+        avec = TPI * np.linalg.inv(bvec).T
+        nmax = (np.sqrt(ecut) * np.linalg.norm(avec, axis=1) / TPI + np.abs(k) + 2).astype(int)
+        r = [np.arange(-nmax[i], nmax[i] + 1) for i in range(3)]
+        g = np.stack(np.meshgrid(*r, indexing="ij"), axis=-1).reshape(-1, 3)
+        kg = (g + k[None, :]) @ bvec
+        e = np.einsum("ij,ij->i", kg, kg)
+        if np.any(np.abs(e - ecut) < 1e-9 * ecut):
+            raise ValueError(f"a plane wave lies on the cutoff sphere at k = {k}")
 
 
 def generate(spec: SynthSpec) -> SynthData:
     rng = np.random.default_rng(spec.seed)
     avec = lattice_vectors(spec.lattice, spec.a)
     bvec, vol = reciprocal(avec)
-    kpts = gamma_mesh(spec.nk)
+    rg, pg, nnp = [np.eye(3, dtype=np.int64)], [np.zeros(3, dtype=np.int64)], 1
+    if spec.sym == "identity":
+        kpts = gamma_mesh(spec.nk)
+    elif spec.sym in ("oh", "oh_glide"):
+        rg, pg, nnp = cubic_point_group(bvec, glide=spec.sym == "oh_glide")
+        kpts = irreducible_mesh(spec.nk, rg)
+        _check_cutoff(bvec, spec.ecut_psi, gamma_mesh(spec.nk))
+    else:
+        raise ValueError(f"unknown symmetry {spec.sym!r}")
     Eev = band_energies(spec, kpts, rng)
     kg, coeffs = [], []
     for ik in range(kpts.shape[0]):
@@ -233,7 +330,38 @@ def generate(spec: SynthSpec) -> SynthData:
         kg.append(G)
         coeffs.append(orthonormal_coeffs(G.shape[0], spec.nbands, rng))
     return SynthData(avec=avec, bvec=bvec, volume=vol, kpts=kpts, kg=kg, coeffs=coeffs,
-                     energies=Eev / AU_EV, efermi=0.0, ecut_psi=spec.ecut_psi)
+                     energies=Eev / AU_EV, efermi=0.0, ecut_psi=spec.ecut_psi, rg=rg, pg=pg, nnp=nnp)
+
+
+def full_mesh_equivalent(d: SynthData) -> SynthData:
+    """The same wave functions as an identity-only input: the full mesh in the
+    order of the reference's unfold of d (chiqw.F:437-480), each point with its
+    make_KG0 plane waves and the coefficients make_C0 gives it
+    (chiqw_sub.F:264-322: C(G) = C_irr(R^-1 (G + RW)) exp(-2 pi i G.pg/nnp),
+    with G negated and the result conjugated for a time-reversed image), and
+    the energies of its irreducible point.  Reading this input unfolds to the
+    same full mesh and the same coefficients, so every chi0 and eps^-1 must
+    agree with d's up to rounding: each time-reversed image follows its
+    partner in the list, and the identity-only unfold rebuilds it from that
+    partner by conjugation, as d's unfold does."""
+    plan = unfold_plan(d.kpts, d.rg)
+    kpts, kg, coeffs, E = [], [], [], []
+    for sk0, ik, iop, trs, RW in plan:
+        G = sphere(d.bvec, d.ecut_psi, sk0)
+        rinv = np.rint(np.linalg.inv(d.rg[iop])).astype(np.int64)
+        pack = {tuple(int(x) for x in g): i for i, g in enumerate(d.kg[ik])}
+        src = G if trs == 1 else -G
+        idx = [pack[tuple(int(x) for x in rinv @ (g + RW))] for g in src]
+        pf = np.exp(-1j * TPI * (src @ d.pg[iop]) / d.nnp)
+        C = d.coeffs[ik][idx, :] * pf[:, None]
+        if trs == -1:
+            C = np.conj(C)
+        kpts.append(sk0)
+        kg.append(G)
+        coeffs.append(np.ascontiguousarray(C))
+        E.append(d.energies[:, ik])
+    return SynthData(avec=d.avec, bvec=d.bvec, volume=d.volume, kpts=np.array(kpts), kg=kg, coeffs=coeffs,
+                     energies=np.stack(E, axis=1), efermi=d.efermi, ecut_psi=d.ecut_psi)
 
 
 def write_dir_wfn(root: str, d: SynthData, ncomp: int = 1):
@@ -249,9 +377,11 @@ def write_dir_wfn(root: str, d: SynthData, ncomp: int = 1):
         for v in d.avec:
             f.write(" ".join(fmt_real(x) for x in v) + "\n")
     with open(os.path.join(w, "dat.symmetry"), "w") as f:
-        f.write("%5d\n%5d\n" % (1, 1))
-        f.write("".join("%3d" % v for v in (1, 0, 0, 0, 1, 0, 0, 0, 1)) + "\n")
-        f.write("%3d%3d%3d\n" % (0, 0, 0))
+        f.write("%5d\n%5d\n" % (len(d.rg), d.nnp))
+        for R, t in zip(d.rg, d.pg):
+            # ((rg(i,j), i=1,3), j=1,3): column by column (chiqw.F:196)
+            f.write("".join("%3d" % int(R[i, j]) for j in range(3) for i in range(3)) + "\n")
+            f.write("%3d%3d%3d\n" % tuple(int(x) for x in t))
     with open(os.path.join(w, "dat.sample-k"), "w") as f:
         f.write("%12d\n" % nk)
         for k in d.kpts:
@@ -331,7 +461,8 @@ def write_dir_wan(root: str, spec: SynthSpec, d: SynthData, full_kg: Optional[Li
     w = os.path.join(root, "dir-wan")
     os.makedirs(w, exist_ok=True)
     rng = np.random.default_rng(spec.seed + 7)
-    nk = d.kpts.shape[0]
+    # dat.ns-nb and dat.umat hold every point of the full mesh (chiqw.F:873-894)
+    nk = int(np.prod(spec.nk))
     nwin = spec.wan_hi - spec.wan_lo + 1
     with open(os.path.join(w, "dat.ns-nb"), "w") as f:
         for _ in range(nk):
@@ -349,6 +480,8 @@ def write_dir_wan(root: str, spec: SynthSpec, d: SynthData, full_kg: Optional[Li
                 f.write(" ".join("(%s,%s)" % (fmt_real(U[ib, jw].real).strip(), fmt_real(U[ib, jw].imag).strip())
                                  for jw in range(nwin)) + "\n")
     if spec.nwf > 0:
+        if len(d.rg) > 1:
+            raise ValueError("synthetic Wannier orbitals are written for identity-only inputs")
         if full_kg is None or full_k is None:
             full_k, full_kg = unfold_full_mesh(d)
         centers = rng.uniform(0.0, 1.0, size=(spec.nwf, 3)) @ d.avec
@@ -380,6 +513,15 @@ def make_case(root: str, spec: SynthSpec, with_wan: bool = True) -> SynthData:
     return d
 
 
+def make_full_mesh_case(root: str, spec: SynthSpec) -> SynthData:
+    """The identity-only input equivalent to the symmetry-reduced case of spec
+    (full_mesh_equivalent), with the same dir-wan."""
+    d = full_mesh_equivalent(generate(spec))
+    write_dir_wfn(root, d)
+    write_dir_wan(root, spec, d)
+    return d
+
+
 # Named synthetic cases used by the tests, the smoke check and the bench.
 CASES = {
     # two-by-two-by-two mesh, small basis: the quick parity case
@@ -397,6 +539,14 @@ CASES = {
                          wan_lo=5, wan_hi=6, nwf=2, wan_sigma=1.0),
     # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
     "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
+    # the cubic point group on an fcc 4x4x4 mesh: 8 irreducible points unfold
+    # to 64 (rotations, time reversal, zone-boundary wraps)
+    "tiny_sym": SynthSpec(nk=(4, 4, 4), nbands=10, nocc=4, ecut_psi=6.3, seed=31, wan_lo=5, wan_hi=6,
+                          shuffle_g=True, sym="oh"),
+    # the same with the diamond structure's fractional translation (nnp = 4)
+    # on half the operations, and a metal with a random cRPA projection
+    "tiny_glide": SynthSpec(nk=(4, 4, 4), nbands=10, nocc=4, ecut_psi=6.3, seed=32, wan_lo=5, wan_hi=6,
+                            shuffle_g=True, sym="oh_glide", metal=True, wan_mode="random"),
     # the 8x8x8-k / 200-band workload's cell, cutoffs and FFT box (fcc a=15.84,
     # 20 Ry, 36^3 box, about 600 G at 11 Ry) on a 4x4x4 mesh with 100 bands
     "headline_small": SynthSpec(lattice="fcc", a=15.84, nk=(4, 4, 4), nbands=100, nocc=8, ecut_psi=20.0,

@@ -106,6 +106,17 @@ class TailMLP:
         self._check(self.L.rp_mlp_train(self._h, _ptr(x), _ptr(t), x.shape[0], steps, batch, lr, _ptr(losses)))
         return losses
 
+    def save(self, path: str, nshell: int, tscale: float = TSCALE) -> None:
+        """Write the network for a context's &param_gpu tail_model: int32 magic
+        "RPTL", version 1, nin, nhid, nout, nshell; float32 tscale and padding;
+        the float32 parameters.  rp_chi0_q then applies the correction on the
+        device, with the shells, features and scale of this module."""
+        hdr = np.array([0x4C545052, 1, self.nin, self.nhid, self.nout, int(nshell)], dtype="<i4")
+        with open(path, "wb") as f:
+            f.write(hdr.tobytes())
+            f.write(np.array([tscale, 0.0], dtype="<f4").tobytes())
+            f.write(self.params().astype("<f4").tobytes())
+
     def close(self):
         if self._h:
             self.L.rp_mlp_destroy(self._h)

@@ -31,7 +31,7 @@ def normwise_err(a: np.ndarray, b: np.ndarray) -> float:
 def run_params(case: str):
     """Namelist values of the parity runs of a synthetic case."""
     kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0)
-    if case == "tiny_metal_crpa":
+    if case in ("tiny_metal_crpa", "tiny_glide"):
         kw["flg_crpa"] = 1
     if case == "config1":
         kw.update(ecut_for_eps=3.0, flg_crpa=1)

@@ -27,7 +27,7 @@ def _oracle_run(root, kw, qidx=None, **extra):
     return orc.calc_chiqw(root, p)
 
 
-@pytest.mark.parametrize("case", ["tiny", "tiny_metal", "tiny_metal_crpa", "tiny_odd"])
+@pytest.mark.parametrize("case", ["tiny", "tiny_metal", "tiny_metal_crpa", "tiny_odd", "tiny_sym", "tiny_glide"])
 def test_chi0_fp64_matches_oracle_all_q(case_dir, fresh_copy, case):
     """Every q point of the case: chi0 within 1e-6 (normwise per frequency),
     eps^-1 within 1e-6 of the oracle's."""
@@ -100,7 +100,8 @@ def test_bad_input_reports_error(case_dir, fresh_copy):
         rp.Context(root + "/nonexistent", rp.default_params(), EM_TEST)
 
 
-@pytest.mark.parametrize("case,qs", [("tiny", [1, 2, 5]), ("tiny_metal", [1, 3]), ("config1", [1, 2, 7])])
+@pytest.mark.parametrize("case,qs", [("tiny", [1, 2, 5]), ("tiny_metal", [1, 3]), ("config1", [1, 2, 7]),
+                                     ("tiny_glide", [1, 4, 8])])
 @pytest.mark.parametrize("pair64", [0, 1])
 @pytest.mark.parametrize("prec", [rp.PREC_FP16X3, rp.PREC_BF16X3, rp.PREC_FP16X2])
 def test_chi0_tensor_core_matches_oracle(case_dir, fresh_copy, case, qs, prec, pair64):
