@@ -521,6 +521,81 @@ def run_ragged(args, steps=None, warmup=None, emit=True):
         shutil.rmtree(tmp, ignore_errors=True)
 
 
+def run_large(args):
+    """The large end-to-end workload on one GPU: fcc a = 15.84 bohr, 10x10x10 k
+    (47 irreducible points of the cubic group in dat.sample-k), 1000 bands
+    (8 occupied: 7936 band pairs), 31.7 Ry (about 2980 plane waves), 48^3 box,
+    dielectric cutoff 25.8 Ry (about 2180 G), 30 frequencies (15 real 0-30 eV,
+    15 imaginary on a Gauss-Legendre grid), FP16x3.  The real-space functions
+    of all 1000 bands would take 885 GB, so the occupied bands stay resident and
+    each pair batch transforms its virtual bands into a window.  A step is one q
+    point; the q points timed are a stated subset of the 47.  The first timed
+    q point's dir-eps is written (its dat.epsqw.600 record is above 2 GiB, in
+    gfortran's subrecords) and read back."""
+    from respackdev_gb300 import build
+    from respackdev_gb300 import chiqw as rp
+    from respackdev_gb300 import synth
+    build.build()
+    tmp = tempfile.mkdtemp(prefix="rp_large_")
+    try:
+        t0 = time.time()
+        synth.make_case(tmp, synth.CASES["large"])
+        gen = time.time() - t0
+        x, _ = np.polynomial.legendre.leggauss(15)
+        em = np.concatenate([np.linspace(0.0, 30.0, 15), 1j * 15.0 * (x + 1.0)]) / AU
+        params = rp.default_params(precision=rp.PREC_FP16X3, fft_box=(48, 48, 48), ecut_for_eps=25.8,
+                                   green_func_delt=0.2721, flg_crpa=1)
+        t0 = time.time()
+        ctx = rp.Context(tmp, params, em)
+        setup = time.time() - t0
+        info = ctx.info()
+        qs = list(range(2, 2 + max(1, args.steps)))
+        per_q, stages, ngs = [], [], []
+        tflops_sus, _, _, src = measured_peaks()
+        alg = 0.0
+        tcg = 0.0
+        with ClockSampler(0) as clk:
+            for iq in qs:
+                t0 = time.perf_counter()
+                ctx.chi0_q(iq, fetch=False)
+                st1 = ctx.stage_times()
+                ctx.epsinv_q(fetch=False)
+                per_q.append(time.perf_counter() - t0)
+                st2 = ctx.stage_times()
+                stages.append({"tetra": st1[0], "pair_density": st1[1], "contraction": st1[2], "eps_inverse": st2[3]})
+                ngs.append(ctx.ng)
+                tcg += ctx.tc_gram_seconds()
+                alg += 8.0 * ctx.ng * ctx.ng * info.n_occ * info.n_vir * info.ntk * info.nen
+        t0 = time.perf_counter()
+        ctx.write_q()
+        write_s = time.perf_counter() - t0
+        rec = os.path.join(tmp, "dir-eps", "q%03d" % qs[-1], "dat.epsqw.600")
+        nbytes = ngs[-1] * ngs[-1] * info.nen * 16
+        ok_size = os.path.getsize(rec) == nbytes + 8 * ((nbytes + 2147483638) // 2147483639)
+        with open(rec, "rb") as f:
+            first_marker = int(np.frombuffer(f.read(4), dtype="<i4")[0])
+        achieved = alg / tcg / 1e12 if tcg > 0 else None
+        line = {"metric": "chiqw s/q-point (all w), large end-to-end workload", "value": float(np.mean(per_q)),
+                "unit": "s/q-point", "n_gpus": 1, "steps": len(qs), "warmup": 0, "higher_is_better": False,
+                "dtype": "fp16x3-split tensor contraction, f32 pair densities, f32-series/f64 weights",
+                "data": "synthetic (seeded generator, 47 irreducible k of the cubic group)",
+                "config": {"workload": "chiqw_10x10x10k_1000b", "ntk": info.ntk, "nk_irr": info.nk_irr,
+                           "nbands": info.ncb, "npair": info.n_occ * info.n_vir, "npw_max": info.ntg,
+                           "ng": ngs, "nen": info.nen, "fft_box": list(info.fft_box), "q_points": qs},
+                "seconds_per_q": per_q, "stage_seconds": stages, "setup_seconds": setup,
+                "input_generation_seconds": gen, "device_bytes": info.device_bytes,
+                "roofline": {"bound": "tensor", "kernel": "tc_gram_kernel", "achieved": achieved, "peak": tflops_sus,
+                             "unit": "TFLOP/s", "frac": achieved / tflops_sus if achieved else None,
+                             "peak_source": f"{src} bf16 sustained"},
+                "eps_record": {"q": qs[-1], "bytes": nbytes, "file_size_ok": ok_size,
+                               "first_marker_negative": first_marker < 0, "write_seconds": write_s},
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+        ctx.close()
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -530,14 +605,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     ap.add_argument("--no-ragged", action="store_true", help="skip the ragged-batch leg of the default line")
-    ap.add_argument("--case", default="full", choices=["full", "small", "ragged"],
+    ap.add_argument("--case", default="full", choices=["full", "small", "ragged", "large"],
                     help="small: 4x4x4 k, 100 bands, same kernels (for profiler captures); "
-                         "ragged: 12 cells' chi0 problems in one grouped launch")
+                         "ragged: 12 cells' chi0 problems in one grouped launch; "
+                         "large: 10x10x10 k, 1000 bands, 48^3 box, about 2180 G (a q subset)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.case == "ragged":
         run_ragged(args)
+    elif args.case == "large":
+        run_large(args)
     else:
         run_gpu(args)
 

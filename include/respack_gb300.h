@@ -73,6 +73,10 @@ typedef struct rp_params {
                                   the FP64 Gauss-Jordan (0: FP32 Gauss-Jordan
                                   plus one float-pair Newton step, FP64 only
                                   as its fallback)                            */
+  int    ur_window;            /* real-space functions of the virtual bands
+                                  held for one pair batch at a time in this
+                                  many slots (0: every band resident when it
+                                  fits in HBM, else as many slots as fit)     */
   char   tail_model[256];      /* band-tail network file (written by
                                   respackdev_gb300.tail.TailMLP.save); when set,
                                   rp_chi0_q adds the network's prediction of

@@ -70,6 +70,13 @@ struct rp_ctx {
   // persistent device data
   DevBuf coef, numirr, trs, src, phase, ng0, kg0, cfull, ur, energy, prob, imt1, index2, em, b9, sk0, errw, inc_off,
       inc;
+  // real-space functions in slots when every band does not fit: the occupied
+  // bands resident (slots 0..n_fixed-1), a window of nwin slots that each pair
+  // batch fills with its virtual bands; h_slot_of / slot_of map band -> slot
+  bool ur_window = false;
+  int n_fixed = 0, nwin = 0, nslot = 0;
+  std::vector<int> h_slot_of;
+  DevBuf slot_of, win_bands;
   // per-q device data
   DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
       rowcol, A, eps, prow, fcol, piv, used, intra, pwpl, mixws, mixaux;
@@ -98,7 +105,7 @@ struct rp_ctx {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &inc_off, &inc, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
                       &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
-                      &intra, &pwpl, &mixws, &mixaux, &tail_sh, &tail_x})
+                      &intra, &pwpl, &mixws, &mixaux, &tail_sh, &tail_x, &slot_of, &win_bands})
       b->release();
     tcw.release();
     if (tail) rp_mlp_destroy(tail);
@@ -270,11 +277,44 @@ static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const do
   RP_CUDA(cudaMemsetAsync(c->errw.p, 0, 16, st));
   const size_t N = (size_t)S.nw[0] * S.nw[1] * S.nw[2];
   c->cfull.ensure(sizeof(cd) * (size_t)S.ntk * S.ncb * S.ntg);
-  c->ur.ensure(sizeof(float) * 2 * (size_t)S.ntk * S.ncb * N);
+  // every band's real-space functions when they fit beside a 48 GB working set
+  // (pair batches, tensor-core operands, eps); otherwise the occupied bands and
+  // a window of virtual bands that each pair batch fills
+  const size_t per_band = sizeof(float) * 2 * (size_t)S.ntk * N;
+  size_t freeb = 0, totb = 0;
+  RP_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const size_t reserve = (size_t)48 << 30;
+  const size_t avail = freeb > reserve ? freeb - reserve : 0;
+  rp::WfnSlots sl;
+  if (p->ur_window > 0 || per_band * (size_t)S.ncb > avail) {
+    c->ur_window = true;
+    c->n_fixed = S.n_occ;
+    int nw = p->ur_window;
+    if (nw <= 0) {
+      // a third of what is left: a window larger than one 24 GB pair batch
+      // can use would only take memory
+      const size_t fixed = per_band * (size_t)c->n_fixed;
+      nw = avail > fixed ? (int)std::min<size_t>((avail - fixed) / 3 / per_band, (size_t)1 << 20) : 0;
+    }
+    c->nwin = std::min(nw, S.ncb - c->n_fixed);
+    if (c->nwin < 1 && S.ncb > c->n_fixed)
+      rp::fail(-2, "device memory holds no window of virtual-band real-space functions (%.1f GB free)",
+               (double)freeb / 1e9);
+    c->nslot = c->n_fixed + std::max(c->nwin, 0);
+    c->h_slot_of.assign(S.ncb, -1);
+    for (int b = 0; b < c->n_fixed; b++) c->h_slot_of[b] = b;
+    upload(c->slot_of, c->h_slot_of, st);
+    sl.slot_of = c->slot_of.as<int>();
+    sl.nslot = c->nslot;
+    c->ur.ensure(per_band * (size_t)c->nslot);
+  } else {
+    c->ur.ensure(per_band * (size_t)S.ncb);
+  }
   c->launches += rp::launch_wfn_realspace(c->coef.as<double2>(), c->numirr.as<int>(), c->trs.as<int>(),
                                           c->src.as<int>(), c->phase.as<double2>(), c->ng0.as<int>(),
                                           c->kg0.as<int>(), S.ntk, S.ncb, S.ntg, S.nw[0], S.nw[1], S.nw[2], c->R[0],
-                                          c->R[1], c->R[2], c->cfull.as<double2>(), c->ur.as<float2>(), 0, S.ntk, st);
+                                          c->R[1], c->R[2], c->cfull.as<double2>(), c->ur.as<float2>(), 0, S.ntk, st,
+                                          sl);
   RP_CUDA(cudaStreamSynchronize(st));
   if (p->tail_model[0]) {
     char path[sizeof p->tail_model + 1];
@@ -376,13 +416,21 @@ static void q_begin(rp_ctx *c, QRun &r) {
   r.ord.resize(npair);
   for (int i = 0; i < npair; i++) r.ord[i] = i;
   std::stable_sort(r.ord.begin(), r.ord.end(), [&](int a, int b) { return t.pair_vir[a] < t.pair_vir[b]; });
+  // With a real-space window, a batch also holds at most nwin virtual bands
+  // outside the resident ones.
   r.bstart.assign(1, 0);
+  int nvb = 0;
   for (int i = 0; i < npair;) {
     int j = i;
     while (j < npair && t.pair_vir[r.ord[j]] == t.pair_vir[r.ord[i]]) j++;  // group [i, j)
     const int cur = i - r.bstart.back();
-    if (cur > 0 && cur + (j - i) > bsz) r.bstart.push_back(i);              // group starts a new batch
+    const bool windowed = c->ur_window && t.pair_vir[r.ord[i]] >= c->n_fixed;
+    if (cur > 0 && (cur + (j - i) > bsz || (windowed && nvb + 1 > c->nwin))) {
+      r.bstart.push_back(i);                                                // group starts a new batch
+      nvb = 0;
+    }
     for (int s0 = i + bsz; s0 < j; s0 += bsz) r.bstart.push_back(s0);      // a group larger than a batch
+    if (windowed) nvb = (j - i > bsz) ? 1 : nvb + 1;
     i = j;
   }
   r.bstart.push_back(npair);
@@ -431,6 +479,29 @@ static void q_batch(rp_ctx *c, QRun &r, int bi, rp::TcWorkspace *ws, bool run_gr
   pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;
   pg.kpq = c->kpq.as<int>(); pg.shift = c->shift.as<int>(); pg.lg0 = c->lg0.as<int>();
   pg.R1 = r.ep[0]; pg.R2 = r.ep[1]; pg.R3 = r.ep[2];
+  if (c->ur_window) {
+    // this batch's virtual bands into the window (counted with the pair densities)
+    std::vector<int> wb;
+    for (int v : cv)
+      if (v >= c->n_fixed && c->h_slot_of[v] < 0 && std::find(wb.begin(), wb.end(), v) == wb.end()) wb.push_back(v);
+    for (int b = c->n_fixed; b < S.ncb; b++) c->h_slot_of[b] = -1;
+    for (size_t i = 0; i < wb.size(); i++) c->h_slot_of[wb[i]] = c->n_fixed + (int)i;
+    if ((int)wb.size() > c->nwin) rp::fail(-2, "pair batch holds %zu virtual bands for %d window slots", wb.size(), c->nwin);
+    upload(c->slot_of, c->h_slot_of, st);
+    upload(c->win_bands, wb, st);
+    rp::WfnSlots sl;
+    sl.bands = c->win_bands.as<int>();
+    sl.nbands = (int)wb.size();
+    sl.slot_of = c->slot_of.as<int>();
+    sl.nslot = c->nslot;
+    sl.rotate = false;
+    c->launches += rp::launch_wfn_realspace(c->coef.as<double2>(), c->numirr.as<int>(), c->trs.as<int>(),
+                                            c->src.as<int>(), c->phase.as<double2>(), c->ng0.as<int>(),
+                                            c->kg0.as<int>(), S.ntk, S.ncb, S.ntg, n1, n2, n3, c->R[0], c->R[1],
+                                            c->R[2], c->cfull.as<double2>(), c->ur.as<float2>(), 0, S.ntk, st, sl);
+    pg.slot_of = c->slot_of.as<int>();
+    pg.nslot = c->nslot;
+  }
   rp::PairChunks pc;
   pc.chunk_vir = c->chunk_vir.as<int>(); pc.chunk_first = c->chunk_first.as<int>();
   pc.chunk_count = c->chunk_count.as<int>(); pc.pair_list = c->pair_list.as<int>();

@@ -75,10 +75,21 @@ template <typename K> inline int smem_cap(K kern) {
 // Full-k coefficients and real-space periodic parts (K1 + K2):
 //   cfull[(k*ncb + b)*ntg + ig] = rotated coefficients (make_C0),
 //   ur[((k*ncb + b)*n3 + z)*n2*n1 + y*n1 + x] = float(bw FFT) (fft3_bw, unscaled).
+// Which (k, band) real-space functions to make and where they go: bands (device
+// list of nbands absolute bands; null = every band), slot_of (device table band
+// -> slot, -1 = none; null = slot b with a stride of ncb bands), nslot (slots
+// per k), rotate (apply make_C0 to coef_irr and write cfull; false: read cfull).
+struct WfnSlots {
+  const int *bands = nullptr;
+  int nbands = 0;
+  const int *slot_of = nullptr;
+  int nslot = 0;
+  bool rotate = true;
+};
 int launch_wfn_realspace(const double2 *coef_irr, const int *numirr, const int *trs, const int *src,
                          const double2 *phase, const int *ng0, const int *kg0, int ntk, int ncb, int ntg,
                          int n1, int n2, int n3, int R1, int R2, int R3, double2 *cfull, float2 *ur,
-                         int k_begin, int k_end, cudaStream_t st);
+                         int k_begin, int k_end, cudaStream_t st, const WfnSlots &sl = WfnSlots());
 
 // Pair densities rho(pair, k, g) = (1/N) DFT[conj(u_vir(k+q)) u_occ(k)] at -G-shift (K3).
 struct PairChunks {
@@ -93,6 +104,10 @@ struct PairGeom {
   int ntk, ncb, n1, n2, n3, ng;
   const int *kpq, *shift, *lg0;  // device
   int R1, R2, R3;                // eps-sphere extent per dimension
+  // real-space functions held in slots: (k, band) at k * nslot + slot_of[band]
+  // (device table); null: every band resident at k * ncb + band
+  const int *slot_of = nullptr;
+  int nslot = 0;
 };
 // out64: rho[(pair*ntk + k)*ng + g] (double2, FP32-rounded values, plain path)
 int launch_pair_density_fp64(const float2 *ur, const PairGeom &g, const PairChunks &c, double2 *out,

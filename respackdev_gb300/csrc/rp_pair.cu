@@ -28,10 +28,18 @@ __device__ __forceinline__ int modp2(int a, int n) { int m = a % n; return m < 0
 
 struct PairArgs {
   int ntk, ncb, n1, n2, n3, ng, R1, R2;
+  // resident real-space functions: (k, band) at slot (k * nslot + slot_of[band]),
+  // or (k * ncb + band) when slot_of is null
+  const int *slot_of;
+  int nslot;
   const int *kpq, *shift, *lg0;
   const int *chunk_vir, *chunk_first, *chunk_count, *pair_list, *pair_occ;
   int jmax;
 };
+
+__device__ __forceinline__ size_t ur_slot(const PairArgs &a, int k, int band) {
+  return a.slot_of ? (size_t)k * a.nslot + a.slot_of[band] : (size_t)k * a.ncb + band;
+}
 
 template <typename T> struct ToT2;
 template <> struct ToT2<double> {
@@ -76,13 +84,13 @@ __global__ void __launch_bounds__(256) pair_density_kernel(const float2 *__restr
   }
   for (int i = tid; i < a.jmax * ng; i += nt) acc[i] = mk<T>(0, 0);
   __syncthreads();
-  const float2 *ui_g = ur + ((size_t)kq * a.ncb + vir) * (size_t)n12 * n3;
+  const float2 *ui_g = ur + ur_slot(a, kq, vir) * (size_t)n12 * n3;
   for (int z = 0; z < n3; z++) {
     for (int i = tid; i < n12; i += nt) ui[i] = ToT2<T>::cvt(ui_g[(size_t)z * n12 + i]);
     __syncthreads();
     for (int jj = 0; jj < cnt; jj++) {
       const int occ = a.pair_occ[a.pair_list[first + jj]];
-      const float2 *uj_g = ur + ((size_t)k * a.ncb + occ) * (size_t)n12 * n3 + (size_t)z * n12;
+      const float2 *uj_g = ur + ur_slot(a, k, occ) * (size_t)n12 * n3 + (size_t)z * n12;
       for (int i = tid; i < n12; i += nt) P[i] = cmul(cconj(ui[i]), ToT2<T>::cvt(uj_g[i]));
       __syncthreads();
       // x pass: X[c1,y] = sum_x P[x,y] TW1[x][c1], two c1 (cc, cc + H1) per thread
@@ -315,7 +323,7 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
     if (tid == 0) tlist[0] = n;
   }
   const size_t bstride = (size_t)n12 * n3;
-  const float2 *uvir = ur + ((size_t)kq * a.ncb + vir) * bstride, *uocc = ur + (size_t)k * a.ncb * bstride;
+  const float2 *uvir = ur + ur_slot(a, kq, vir) * bstride;
   // the virtual band is read by this CTA alone, straight from HBM: its slab two
   // ahead is pulled into L2 by one bulk prefetch per slab (16-byte multiples)
   const bool pf = (n12 % 2) == 0;
@@ -329,7 +337,7 @@ __global__ void __launch_bounds__(PD_THREADS, 2) pair_slab_kernel(const float2 *
     for (int row = tid; row < cnt * n1; row += PD_THREADS) {
       const int j1 = row / n1, x1 = row - j1 * n1;
       const float2 *pv = uvir + x1;
-      const float2 *pa = uocc + (size_t)a.pair_occ[a.pair_list[first + j1]] * bstride + x1;
+      const float2 *pa = ur + ur_slot(a, k, a.pair_occ[a.pair_list[first + j1]]) * bstride + x1;
       const size_t zo = (size_t)z * n12;
       for (int cg = 0; cg < D2; cg += CG) {
         float2 sa[CG];
@@ -489,6 +497,7 @@ size_t pair_density_smem(const PairGeom &g, int jmax, bool fp64) {
 static PairArgs pair_args(const PairGeom &g, const PairChunks &c) {
   PairArgs a;
   a.ntk = g.ntk; a.ncb = g.ncb; a.n1 = g.n1; a.n2 = g.n2; a.n3 = g.n3; a.ng = g.ng; a.R1 = g.R1; a.R2 = g.R2;
+  a.slot_of = g.slot_of; a.nslot = g.nslot;
   a.kpq = g.kpq; a.shift = g.shift; a.lg0 = g.lg0;
   a.chunk_vir = c.chunk_vir; a.chunk_first = c.chunk_first; a.chunk_count = c.chunk_count;
   a.pair_list = c.pair_list; a.pair_occ = c.pair_occ; a.jmax = c.jmax;

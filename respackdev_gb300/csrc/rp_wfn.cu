@@ -15,6 +15,12 @@
 // The transform is three separable DFT passes over one output z-slab at a
 // time, staged in shared memory: the plane-wave sphere sits in a compact
 // (2R+1)^3 cube, so the z pass touches only the sphere's bounding box.
+//
+// When the real-space functions of every band do not fit in HBM (1000 k x
+// 1000 bands on a 48^3 box would take 885 GB), the context keeps the occupied
+// bands resident and transforms each pair batch's virtual bands into a window
+// of slots when the batch starts (WfnSlots: a band list, their slots, and
+// rotate = false to start from the rotated coefficients kept in cfull).
 #include "rp_dev.cuh"
 #include "rp_host.h"
 
@@ -26,9 +32,13 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     const double2 *__restrict__ coef_irr, const int *__restrict__ numirr, const int *__restrict__ trs,
     const int *__restrict__ src, const double2 *__restrict__ phase, const int *__restrict__ ng0,
     const int *__restrict__ kg0, int ncb, int ntg, int n1, int n2, int n3, int R1, int R2, int R3,
-    double2 *__restrict__ cfull, float2 *__restrict__ ur, int k_begin) {
+    double2 *__restrict__ cfull, float2 *__restrict__ ur, int k_begin, WfnSlots sl) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int b = blockIdx.x, k = k_begin + blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  const int b = sl.bands ? sl.bands[blockIdx.x] : blockIdx.x;
+  const int k = k_begin + blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+  // the slot of (k, b) in ur; a band without a slot only gets its coefficients
+  const int slot = sl.slot_of ? sl.slot_of[b] : b;
+  const size_t ur_at = (size_t)k * (sl.slot_of ? sl.nslot : ncb) + slot;
   const bool c1 = 2 * R1 + 1 <= n1, c2 = 2 * R2 + 1 <= n2, c3 = 2 * R3 + 1 <= n3;
   const int D1 = c1 ? 2 * R1 + 1 : n1, D2 = c2 ? 2 * R2 + 1 : n2, D3 = c3 ? 2 * R3 + 1 : n3;
   double2 *cube = (double2 *)smem;                 // D1*D2*D3, index c1 + D1*(c2 + D2*c3)
@@ -44,26 +54,31 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
   for (int j = tid; j < D2; j += nt) f2[j] = c2 ? modp(j - R2, n2) : j;
   for (int j = tid; j < D3; j += nt) f3[j] = c3 ? modp(j - R3, n3) : j;
   __syncthreads();
-  // 1. rotate + scatter into the cube
+  // 1. rotate (or take the rotated coefficients) + scatter into the cube
   const int ikir = numirr[k], t = trs[k], ng = ng0[k];
   const double2 *cirr = coef_irr + ((size_t)ikir * ncb + b) * ntg;
   double2 *cf = cfull + ((size_t)k * ncb + b) * ntg;
   for (int ig = tid; ig < ntg; ig += nt) {
     double2 v = make_double2(0, 0);
     if (ig < ng) {
-      int s = src[(size_t)k * ntg + ig];
-      v = cmul(cirr[s], phase[(size_t)k * ntg + ig]);
-      if (t == -1) v.y = -v.y;
+      if (sl.rotate) {
+        int s = src[(size_t)k * ntg + ig];
+        v = cmul(cirr[s], phase[(size_t)k * ntg + ig]);
+        if (t == -1) v.y = -v.y;
+      } else {
+        v = cf[ig];
+      }
       const int *g = kg0 + ((size_t)k * ntg + ig) * 3;
       int i1 = c1 ? g[0] + R1 : modp(g[0], n1);
       int i2 = c2 ? g[1] + R2 : modp(g[1], n2);
       int i3 = c3 ? g[2] + R3 : modp(g[2], n3);
       cube[i1 + D1 * (i2 + D2 * i3)] = v;
     }
-    cf[ig] = v;
+    if (sl.rotate) cf[ig] = v;
   }
+  if (slot < 0) return;  // uniform over the block: no barrier is skipped by part of it
   __syncthreads();
-  float2 *out = ur + ((size_t)k * ncb + b) * (size_t)n1 * n2 * n3;
+  float2 *out = ur + ur_at * (size_t)n1 * n2 * n3;
   for (int z = 0; z < n3; z++) {
     // pass z: A[c1,c2] = sum_c3 cube e^{+2 pi i f3 z / n3}
     for (int o = tid; o < D1 * D2; o += nt) {
@@ -97,17 +112,20 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
 int launch_wfn_realspace(const double2 *coef_irr, const int *numirr, const int *trs, const int *src,
                          const double2 *phase, const int *ng0, const int *kg0, int ntk, int ncb, int ntg,
                          int n1, int n2, int n3, int R1, int R2, int R3, double2 *cfull, float2 *ur,
-                         int k_begin, int k_end, cudaStream_t st) {
+                         int k_begin, int k_end, cudaStream_t st, const WfnSlots &sl) {
   (void)ntk;
+  const int nb = sl.bands ? sl.nbands : ncb;
+  if (nb == 0 || k_end <= k_begin) return 0;
   const int D1 = 2 * R1 + 1 <= n1 ? 2 * R1 + 1 : n1, D2 = 2 * R2 + 1 <= n2 ? 2 * R2 + 1 : n2,
             D3 = 2 * R3 + 1 <= n3 ? 2 * R3 + 1 : n3;
   size_t smem = sizeof(double2) * ((size_t)D1 * D2 * D3 + D1 * D2 + D1 * n2 + n1 + n2 + n3) +
                 sizeof(int) * (D1 + D2 + D3);
-  if (smem > 200 * 1024) fail(1, "plane-wave sphere too large for the shared-memory cube (%zu bytes)", smem);
-  RP_CUDA(cudaFuncSetAttribute(wfn_realspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_cap(wfn_realspace_kernel)));
-  dim3 grid(ncb, k_end - k_begin);
+  const int cap = smem_cap(wfn_realspace_kernel);
+  if (smem > (size_t)cap) fail(1, "plane-wave sphere too large for the shared-memory cube (%zu bytes)", smem);
+  RP_CUDA(cudaFuncSetAttribute(wfn_realspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+  dim3 grid(nb, k_end - k_begin);
   wfn_realspace_kernel<<<grid, 256, smem, st>>>(coef_irr, numirr, trs, src, phase, ng0, kg0, ncb, ntg, n1, n2,
-                                                n3, R1, R2, R3, cfull, ur, k_begin);
+                                                n3, R1, R2, R3, cfull, ur, k_begin, sl);
   RP_CUDA(cudaGetLastError());
   return 1;
 }

@@ -17,9 +17,13 @@ exact formats the reference reads:
 
 Units follow the reference: lengths in bohr, band energies and the Fermi
 level in Hartree, the wave-function cutoff in Rydberg (|k+G|^2 in bohr^-2).
-The symmetry file lists the identity only, and the sample-k list holds the
-whole Gamma-centred mesh, so the reference's unfolding (time reversal
-included, ``chiqw.F:437-480``) reproduces the mesh.
+By default the symmetry file lists the identity only and the sample-k list
+holds the whole Gamma-centred mesh, so the reference's unfolding (time
+reversal included, ``chiqw.F:437-480``) reproduces the mesh.  With
+``sym="oh"`` / ``"oh_glide"`` it lists the 48 cubic operations (with the
+diamond structure's fractional translation on half of them) and only the
+irreducible points, as a DFT converter writes them; ``full_mesh_equivalent``
+gives the identity-only input with the same unfolded wave functions.
 """
 from __future__ import annotations
 
@@ -257,8 +261,10 @@ def cubic_point_group(bvec: np.ndarray, glide: bool = False):
     return [o[1] for o in ops], [o[2] for o in ops], (4 if glide else 1)
 
 
-def _kmatch(a: np.ndarray, b: np.ndarray) -> bool:
-    return bool(np.all(np.abs(a - b) < 1.0e-4))
+def _kkey(k: np.ndarray):
+    """Hash key of a mesh point: the reference compares k points to 1e-4
+    (chiqw.F:452-455); mesh coordinates are far apart on that scale."""
+    return tuple(int(x) for x in np.rint(np.asarray(k) * 1.0e4))
 
 
 def unfold_plan(kirr: np.ndarray, rg: List[np.ndarray]):
@@ -266,14 +272,16 @@ def unfold_plan(kirr: np.ndarray, rg: List[np.ndarray]):
     (chiqw.F:437-480): per irreducible k and operation the image R k folded by
     kcheck, then its time-reversed image folded by kcheck_trs, each kept when
     new.  Returns [(SK0, numirr, numrot, trs, RW)] in that order (0-based)."""
-    out = []
+    out, seen = [], set()
     for ik in range(kirr.shape[0]):
         for iop, R in enumerate(rg):
             kt, RW = _kcheck(R @ kirr[ik], False)
-            if not any(_kmatch(o[0], kt) for o in out):
+            if _kkey(kt) not in seen:
+                seen.add(_kkey(kt))
                 out.append((kt, ik, iop, 1, RW))
             kt, RW = _kcheck(R @ kirr[ik], True)
-            if not any(_kmatch(o[0], -kt) for o in out):
+            if _kkey(-kt) not in seen:
+                seen.add(_kkey(-kt))
                 out.append((-kt, ik, iop, -1, RW))
     return out
 
@@ -283,13 +291,15 @@ def irreducible_mesh(nk: Sequence[int], rg: List[np.ndarray]) -> np.ndarray:
     the first of each star in mesh order, such that unfold_plan covers the mesh."""
     mesh = gamma_mesh(nk)
     kept: List[np.ndarray] = []
-    covered: List[np.ndarray] = []
+    covered = set()
     for k in mesh:
-        if any(_kmatch(c, k) for c in covered):
+        if _kkey(k) in covered:
             continue
         kept.append(k)
-        covered = [o[0] for o in unfold_plan(np.array(kept), rg)]
-    if len(covered) != mesh.shape[0]:
+        for R in rg:
+            covered.add(_kkey(_kcheck(R @ k, False)[0]))
+            covered.add(_kkey(-_kcheck(R @ k, True)[0]))
+    if len(unfold_plan(np.array(kept), rg)) != mesh.shape[0]:
         raise ValueError("the operations do not map the mesh onto itself")
     return np.array(kept)
 
@@ -537,6 +547,9 @@ CASES = {
                           wan_lo=5, wan_hi=7, nwf=3, wan_sigma=1.2),
     "odd_wan": SynthSpec(nk=(3, 3, 3), nbands=10, nocc=4, ecut_psi=6.0, seed=23,
                          wan_lo=5, wan_hi=6, nwf=2, wan_sigma=1.0),
+    # five Gaussian Wannier orbitals on a 3x3x3 mesh with 24 bands (static U/J)
+    "wan5": SynthSpec(nk=(3, 3, 3), nbands=24, nocc=4, ecut_psi=8.0, seed=25,
+                      wan_lo=5, wan_hi=9, nwf=5, wan_sigma=1.1),
     # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
     "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
     # the cubic point group on an fcc 4x4x4 mesh: 8 irreducible points unfold
@@ -554,4 +567,12 @@ CASES = {
     # the 8x8x8-k / 200-band workload itself
     "headline": SynthSpec(lattice="fcc", a=15.84, nk=(8, 8, 8), nbands=200, nocc=8, ecut_psi=20.0,
                           seed=2024, wan_lo=9, wan_hi=11, shuffle_g=False),
+    # the large end-to-end workload: 10x10x10 k (47 irreducible points under the
+    # cubic group), 1000 bands, 31.7 Ry (about 2980 plane waves; 48^3 box),
+    # dielectric cutoff 25.8 Ry (about 2180 G)
+    "large": SynthSpec(lattice="fcc", a=15.84, nk=(10, 10, 10), nbands=1000, nocc=8, ecut_psi=31.7,
+                       seed=2025, wan_lo=9, wan_hi=11, shuffle_g=False, sym="oh"),
+    # its cell, cutoffs and box on a 2x2x2 mesh with 40 bands (parity case)
+    "large_small": SynthSpec(lattice="fcc", a=15.84, nk=(2, 2, 2), nbands=40, nocc=8, ecut_psi=31.7,
+                             seed=2026, wan_lo=9, wan_hi=11, shuffle_g=False, sym="oh"),
 }

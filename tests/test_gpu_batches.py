@@ -23,3 +23,21 @@ def test_pair_batches_agree(case_dir, fresh_copy, prec, tol):
         for (chi, eps), (chi0, eps0) in zip(res[pb], res[0]):
             assert normwise_err(chi, chi0) < tol
             assert normwise_err(eps, eps0) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [(rp.PREC_FP64, 1e-12), (rp.PREC_FP16X3, 1e-7)])
+def test_real_space_window_gives_the_same_chi0(case_dir, fresh_copy, prec, tol):
+    """With ur_window the context keeps only the occupied bands' real-space
+    functions resident and transforms each pair batch's virtual bands into a
+    window of slots (here 3, so a q takes several batches); chi0 and eps^-1
+    equal those of the context that holds every band, up to the order of the
+    pair sums."""
+    kw = run_params("tiny_metal")
+    root = fresh_copy(case_dir("tiny_metal"))
+    out = {}
+    for win in (0, 3):
+        with rp.Context(root, rp.default_params(precision=prec, ur_window=win, **kw), EM_TEST) as ctx:
+            out[win] = [(ctx.chi0_q(iq), ctx.epsinv_q()) for iq in (1, 2, 5)]
+    for (c0, e0), (c1, e1) in zip(out[0], out[3]):
+        assert normwise_err(c1, c0) < tol
+        assert normwise_err(e1, e0) < tol

@@ -148,3 +148,35 @@ def test_mvmc_files_match_oracle_writer(int_case, int_copy, tmp_path):
         v2 = np.array([v for _, v in r2])
         assert r2, name
         assert np.abs(v1 - v2).max() <= TOL * np.abs(v2).max() + 1e-9, name
+
+
+def test_static_uj_of_the_fast_path_within_5_mev(int_case, int_copy):
+    """Five Gaussian Wannier orbitals: dir-eps from the split-precision chiqw
+    (FP16x3 contraction, FP32-series tetrahedron weights, mixed-precision
+    inverse) and the GPU calc_int, against the oracle's FP64 chiqw and calc_int.
+    The static U (W at R = 0, w = 0) and J (J at R = 0, w = 0) agree within
+    the 5 meV the fast path is held to (they agree far better)."""
+    import shutil
+    from respackdev_gb300 import chiqw as rp
+    from tests.helpers import EM_INT, namelist_text
+    src = int_case("wan5")
+    AU = 27.21151
+    dims, ref = orc.calc_int(src, orc.make_int_params(nthreads=8, ix_min=0, ix_max=1, write_files=0))
+    root = int_copy(src)
+    shutil.rmtree(os.path.join(root, "dir-eps"))
+    rp.calc_chiqw(root, namelist_text(dict(green_func_delt=0.2721, ecut_for_eps=3.0), EM_INT, "precision='fp16x3'"))
+    p = ci.default_params(ix_intj_min=0, ix_intj_max=1, write_files=0)
+    with ci.IntContext(root, p) as c:
+        assert c.nwf == 5
+        V, W = c.w3d()
+        X, J = c.j3d()
+    c0 = tuple(dims.na)
+    U_gpu, U_ref = W[:, :, c0[0], c0[1], c0[2], 0], ref["W"][:, :, c0[0], c0[1], c0[2], 0]
+    J_gpu, J_ref = J[:, :, c0[0], c0[1], c0[2], 0], ref["J"][:, :, c0[0], c0[1], c0[2], 0]
+    du = float(np.abs(U_gpu - U_ref).max()) * AU * 1e3
+    dj = float(np.abs(J_gpu - J_ref).max()) * AU * 1e3
+    print(f"static U/J, 5 orbitals: max |dU| {du:.3e} meV, max |dJ| {dj:.3e} meV "
+          f"(U up to {np.abs(U_ref).max() * AU:.3f} eV)")
+    assert du < 5.0 and dj < 5.0
+    # the bare V does not depend on eps^-1: the GPU's equals the oracle's
+    assert _rel(V, ref["V"]) < TOL
