@@ -73,6 +73,10 @@ typedef struct rp_params {
                                   the FP64 Gauss-Jordan (0: FP32 Gauss-Jordan
                                   plus one float-pair Newton step, FP64 only
                                   as its fallback)                            */
+  int    tetra_fp64;           /* 1: the split precisions also take the
+                                  reference's FP64 closed forms for every
+                                  tetrahedron weight (0: the FP32 series where
+                                  it converges)                               */
   int    ur_window;            /* real-space functions of the virtual bands
                                   held for one pair batch at a time in this
                                   many slots (0: every band resident when it

@@ -473,7 +473,7 @@ static void q_batch(rp_ctx *c, QRun &r, int bi, rp::TcWorkspace *ws, bool run_gr
   RP_CUDA(cudaEventRecord(c->ev[0], st));
   // the split precisions take the FP32 series where it converges; the plain
   // FP64 path keeps the reference's closed forms everywhere
-  c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st, r.fast);
+  c->launches += rp::launch_tetra_weights(ta, c->wts.as<double2>(), st, r.fast && !S.params.tetra_fp64);
   RP_CUDA(cudaEventRecord(c->ev[1], st));
   rp::PairGeom pg;
   pg.ntk = ntk; pg.ncb = S.ncb; pg.n1 = n1; pg.n2 = n2; pg.n3 = n3; pg.ng = ng;

@@ -291,6 +291,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "write_eps_f32") p->write_eps_f32 = nl_int(v, k);
       else if (k == "eps_fp64") p->eps_fp64 = nl_int(v, k);
       else if (k == "ur_window") p->ur_window = nl_int(v, k);
+      else if (k == "tetra_fp64") p->tetra_fp64 = nl_int(v, k);
       else if (k == "tail_model") {
         const std::string path = v.empty() ? "" : v[0];
         if (path.size() >= sizeof p->tail_model) fail(1, "&param_gpu tail_model: path longer than %zu characters",

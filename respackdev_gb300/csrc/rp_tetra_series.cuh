@@ -117,44 +117,54 @@ static const float kTsA[TS_NMAX] = {RP_TS_A5(0), RP_TS_A5(5), RP_TS_A5(10), RP_T
 // is w - gbar - i delt.  ok[s] says whether the series was taken for sign s
 // (s = 0: +1, s = 1: -1): false where r > TS_RMAX or z = 0, x[s] then 0.
 // Values in the closed forms' normalisation (before the factor fk = dsgn).
+//
+// Near resonance |z| is of order delt and u^n alone would overflow FP32 (and
+// h_n underflow) long before their product, which r^n bounds, is small.  So
+// with sc = 1/min|z| over the signs taken, the recurrences run on d sc
+// (|d sc| <= r) and u / sc (|u / sc| <= 1): h_n(d) u^n = h_n(d sc) (u / sc)^n.
 RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, double mean, double delt, double wr,
                                    double wi, bool (&ok)[2], TsCplx (&x)[2]) {
-  float ur[2], ui[2], rmax = 0.f;
+  float zr[2], zi[2], inv[2], sc = 0.f;
   for (int s = 0; s < 2; s++) {
     const double sg = s == 0 ? 1.0 : -1.0;
     // z in double (one subtraction's worth of care), the rest in FP32
-    const float zr = (float)(wr + sg * mean), zi = (float)(wi + sg * delt);
-    const float zz = zr * zr + zi * zi;
+    zr[s] = (float)(wr + sg * mean);
+    zi[s] = (float)(wi + sg * delt);
+    const float zz = zr[s] * zr[s] + zi[s] * zi[s];
     ok[s] = zz > 0.f && dmax * dmax <= TS_RMAX * TS_RMAX * zz;
-    const float inv = ok[s] ? 1.f / zz : 0.f;
-    ur[s] = zr * inv;
-    ui[s] = -zi * inv;
-    if (ok[s]) rmax = fmaxf(rmax, dmax * sqrtf(inv));
+    inv[s] = ok[s] ? 1.f / zz : 0.f;
+    if (ok[s]) sc = fmaxf(sc, sqrtf(inv[s]));
     x[s] = TsCplx{0.f, 0.f};
   }
   if (!ok[0] && !ok[1]) return;
-  // n = 0: a_0 u
-  float pr0 = ur[0], pi0 = ui[0], pr1 = ur[1], pi1 = ui[1];
-  float sr0 = kTsA[0] * pr0, si0 = kTsA[0] * pi0, sr1 = kTsA[0] * pr1, si1 = kTsA[0] * pi1;
+  // scaled u = conj(z) / |z|^2 / sc of each sign, and the scaled deviations
+  const float is = 1.f / sc;
+  const float ur0 = zr[0] * inv[0] * is, ui0 = -zi[0] * inv[0] * is;
+  const float ur1 = zr[1] * inv[1] * is, ui1 = -zi[1] * inv[1] * is;
+  const float e0 = d[0] * sc, e1 = d[1] * sc, e2 = d[2] * sc, e3 = d[3] * sc, ev = dv * sc;
+  const float rmax = dmax * sc;
+  // S_s = sum_n a_n h_n(d sc) (u_s / sc)^n; n = 0 term a_0
+  float pr0 = 1.f, pi0 = 0.f, pr1 = 1.f, pi1 = 0.f;
+  float sr0 = kTsA[0], si0 = 0.f, sr1 = kTsA[0], si1 = 0.f;
   float h1 = 1.f, h2 = 1.f, h3 = 1.f, h4 = 1.f, hv = 1.f;
   // term n is at most r^n times the first: take terms while r^(n-1) > 2^-24
   float rprev = 1.f;
   float sgn = 1.f;
   for (int n = 1; n < TS_NMAX && rprev > 5.9604645e-8f; n++) {
-    h1 = d[0] * h1;
-    h2 = h1 + d[1] * h2;
-    h3 = h2 + d[2] * h3;
-    h4 = h3 + d[3] * h4;
-    hv = h4 + dv * hv;
+    h1 = e0 * h1;
+    h2 = h1 + e1 * h2;
+    h3 = h2 + e2 * h3;
+    h4 = h3 + e3 * h4;
+    hv = h4 + ev * hv;
     sgn = -sgn;
     const float t = sgn * kTsA[n] * hv;
-    float q = pr0 * ur[0] - pi0 * ui[0];
-    pi0 = pr0 * ui[0] + pi0 * ur[0];
+    float q = pr0 * ur0 - pi0 * ui0;
+    pi0 = pr0 * ui0 + pi0 * ur0;
     pr0 = q;
     sr0 += t * pr0;
     si0 += t * pi0;
-    q = pr1 * ur[1] - pi1 * ui[1];
-    pi1 = pr1 * ui[1] + pi1 * ur[1];
+    q = pr1 * ur1 - pi1 * ui1;
+    pi1 = pr1 * ui1 + pi1 * ur1;
     pr1 = q;
     // sign -1: its d are negated, so its h_n carry (-1)^n
     const float t1 = (n & 1) ? -t : t;
@@ -162,8 +172,15 @@ RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, do
     si1 += t1 * pi1;
     rprev *= rmax;
   }
-  if (ok[0]) x[0] = TsCplx{sr0, si0};
-  if (ok[1]) x[1] = TsCplx{sr1, si1};
+  // x_s = u_s S_s, u_s = conj(z_s) / |z_s|^2
+  if (ok[0]) {
+    const float ar = zr[0] * inv[0], ai = -zi[0] * inv[0];
+    x[0] = TsCplx{ar * sr0 - ai * si0, ar * si0 + ai * sr0};
+  }
+  if (ok[1]) {
+    const float ar = zr[1] * inv[1], ai = -zi[1] * inv[1];
+    x[1] = TsCplx{ar * sr1 - ai * si1, ar * si1 + ai * sr1};
+  }
 }
 
 }  // namespace rp

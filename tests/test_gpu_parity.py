@@ -140,19 +140,19 @@ def test_gen_grid_matches_oracle(case_dir, fresh_copy, tmp_path):
     from respackdev_gb300 import build
     kw = run_params("tiny")
     ref_root = fresh_copy(case_dir("tiny"))
-    orc.calc_chiqw(ref_root, orc.make_params(dump_chi=1, nthreads=8, calc_num_k=[2], num_freq_grid=12, **kw))
+    orc.calc_chiqw(ref_root, orc.make_params(dump_chi=1, nthreads=8, calc_num_k=[2], num_freq_grid=20, **kw))
     run = str(tmp_path / "run")
     shutil.copytree(os.path.join(case_dir("tiny"), "dir-wfn"), os.path.join(run, "dir-wfn"))
     # &param_chiqw, then the q list (m_rdinput.f90:97-103), then &param_gpu
-    text = namelist_text(dict(kw, num_freq_grid=12, flg_calc_type=2, n_calc_q=1)) + " 2\n&param_gpu dump_chi=1 /\n"
+    text = namelist_text(dict(kw, num_freq_grid=20, flg_calc_type=2, n_calc_q=1)) + " 2\n&param_gpu dump_chi=1 /\n"
     r = subprocess.run([build.EXE], input=text, text=True, cwd=run, capture_output=True)
     assert r.returncode == 0, r.stderr
     w1 = open(os.path.join(run, "dir-eps", "dat.wgrid")).read()
     w2 = open(os.path.join(ref_root, "dir-eps", "dat.wgrid")).read()
     assert w1 == w2
     g1 = np.loadtxt(os.path.join(run, "dir-eps", "dat.wgrid"), skiprows=1)
-    assert g1.shape == (12, 2) and np.all(np.diff(g1[:, 0]) > 0)
+    assert g1.shape == (20, 2) and np.all(np.diff(g1[:, 0]) > 0)
     chi = orc.read_chi_dump(os.path.join(run, "dir-eps", "q002", "dat.chi0"))
     ref = orc.read_chi_dump(os.path.join(ref_root, "dir-eps", "q002", "dat.chi0"))
-    assert chi.shape == ref.shape and chi.shape[2] == 12
+    assert chi.shape == ref.shape and chi.shape[2] == 20
     assert normwise_err(chi, ref) < 1e-6

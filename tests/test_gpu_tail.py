@@ -76,11 +76,14 @@ def _cell(seed: int):
     with rp.Context(root, rp.default_params(n_calc_band=NTRUNC, **kw), EM) as ct, \
             rp.Context(root, rp.default_params(n_calc_band=NFULL, **kw), EM) as cf:
         for iq in QS:
-            q = d.kpts[iq - 1]
-            LG = synth.sphere(d.bvec, 3.0, q)
-            ql = np.linalg.norm((LG + q[None, :]) @ d.bvec, axis=1)
             chi_t = ct.chi0_q(iq)[..., 0]
             chi_f = cf.chi0_q(iq)[..., 0]
+            # |q+G| in the library's G order, from the q it writes to dat.sq
+            ct.epsinv_q(fetch=False)
+            ct.write_q()
+            q = np.loadtxt(os.path.join(root, "dir-eps", "q%03d" % iq, "dat.sq"))
+            LG = synth.sphere(d.bvec, 3.0, q)
+            ql = np.linalg.norm((LG + q[None, :]) @ d.bvec, axis=1)
             assert chi_t.shape[0] == len(LG)
             out.append((chi_t, chi_f, ql))
     return stats, out
@@ -124,7 +127,7 @@ def test_tail_correction_in_the_product_path(cells, tmp_path):
     and eps^-1 from the corrected chi0 is closer to the full-band eps^-1 than
     eps^-1 of the truncated sum.  rp_epsinv_chi_q inverts a caller chi0: given
     the host-corrected chi0 it returns the same eps^-1."""
-    train, held = cells[:6], cells[6:]
+    train = cells[:6]
     X, T = [], []
     for stats, qs in train:
         for chi_t, chi_f, ql in qs:
@@ -132,37 +135,41 @@ def test_tail_correction_in_the_product_path(cells, tmp_path):
             T.append(tail.targets(chi_t, chi_f, ql, NSHELL))
     X, T = np.concatenate(X), np.concatenate(T)
     model = str(tmp_path / "dat.tail")
+    kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0, precision=rp.PREC_FP64)
+    e_trunc, e_corr = [], []
     with tail.TailMLP(seed=3) as m:
         m.train(X, T, steps=3000, batch=128, lr=1e-3)
         m.save(model, NSHELL)
-        held_pred = []
-        for stats, qs in held:
-            held_pred.append([m.forward(tail.features(chi_t, ql, EM, stats, NSHELL)[0]) for chi_t, _, ql in qs])
-    kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0, precision=rp.PREC_FP64)
-    e_trunc, e_corr = [], []
-    for h, seed in enumerate((106, 107)):
-        spec = dataclasses.replace(synth.CASES["tiny"], nbands=NFULL, seed=seed)
-        root = tempfile.mkdtemp(prefix="rp_tailp_")
-        synth.make_case(root, spec)
-        with rp.Context(root, rp.default_params(n_calc_band=NTRUNC, tail_model=model, **kw), EM) as cc, \
-                rp.Context(root, rp.default_params(n_calc_band=NTRUNC, **kw), EM) as ct, \
-                rp.Context(root, rp.default_params(n_calc_band=NFULL, **kw), EM) as cf:
-            for i, iq in enumerate(QS):
-                chi_c = cc.chi0_q(iq)
-                assert cc.tail_applied() and not ct.tail_applied()
-                eps_c = cc.epsinv_q()
-                chi_t = ct.chi0_q(iq)
-                eps_t = ct.epsinv_q()
-                cf.chi0_q(iq)
-                eps_f = cf.epsinv_q()
-                _, _, ql = held[h][1][i]
-                chi_h = tail.apply(chi_t[..., 0], held_pred[h][i], ql, NSHELL)
-                assert _rel(chi_c[..., 0], chi_h) < 1e-5
-                # the host-corrected chi0 through rp_epsinv_chi_q gives the same eps^-1
-                eps_h = ct.epsinv_chi_q(chi_h)
-                assert _rel(eps_h, eps_c) < 1e-5
-                e_trunc.append(_rel(eps_t, eps_f))
-                e_corr.append(_rel(eps_c, eps_f))
+        for seed in (106, 107):       # the held-out cells
+            spec = dataclasses.replace(synth.CASES["tiny"], nbands=NFULL, seed=seed)
+            root = tempfile.mkdtemp(prefix="rp_tailp_")
+            d = synth.make_case(root, spec)
+            stats = tail.band_stats(d.energies, d.efermi, NTRUNC)
+            with rp.Context(root, rp.default_params(n_calc_band=NTRUNC, tail_model=model, **kw), EM) as cc, \
+                    rp.Context(root, rp.default_params(n_calc_band=NTRUNC, **kw), EM) as ct, \
+                    rp.Context(root, rp.default_params(n_calc_band=NFULL, **kw), EM) as cf:
+                for iq in QS:
+                    chi_c = cc.chi0_q(iq)
+                    assert cc.tail_applied() and not ct.tail_applied()
+                    eps_c = cc.epsinv_q()
+                    chi_t = ct.chi0_q(iq)
+                    eps_t = ct.epsinv_q()
+                    cf.chi0_q(iq)
+                    eps_f = cf.epsinv_q()
+                    # |q+G| in the library's G order, from the q it writes to dat.sq
+                    ct.write_q()
+                    q = np.loadtxt(os.path.join(root, "dir-eps", "q%03d" % iq, "dat.sq"))
+                    LG = synth.sphere(d.bvec, 3.0, q)
+                    ql = np.linalg.norm((LG + q[None, :]) @ d.bvec, axis=1)
+                    assert len(ql) == chi_t.shape[0]
+                    pred = m.forward(tail.features(chi_t[..., 0], ql, EM, stats, NSHELL)[0])
+                    chi_h = tail.apply(chi_t[..., 0], pred, ql, NSHELL)
+                    assert _rel(chi_c[..., 0], chi_h) < 1e-5
+                    # the host-corrected chi0 through rp_epsinv_chi_q gives the same eps^-1
+                    eps_h = ct.epsinv_chi_q(chi_h)
+                    assert _rel(eps_h, eps_c) < 1e-5
+                    e_trunc.append(_rel(eps_t, eps_f))
+                    e_corr.append(_rel(eps_c, eps_f))
     et, ec = float(np.mean(e_trunc)), float(np.mean(e_corr))
     print(f"held-out eps^-1 error: truncated {et:.3e}, tail-corrected (device) {ec:.3e} ({et / ec:.1f}x smaller)")
     assert ec < et

@@ -119,11 +119,32 @@ def test_series_weights_match_the_closed_forms(tmp_path):
 
 HARNESS2 = r"""
 #include <cmath>
+#include <complex>
 #include <cstdio>
 #include <random>
 #include "rp_tetra_series.cuh"
+typedef std::complex<long double> C;
+static C lr(C a, C b) {
+  const C t = (a - b) / b;
+  return C(0.5L * std::log1p(2.0L * t.real() + std::norm(t)), std::atan2(t.imag(), 1.0L + t.real()));
+}
+static C s2(C g0, C g1, C g2, C g3, C w) {
+  C v = -(g1 + w) * (g1 + w) / (6.0L * (g0 - g1) * (g1 - g2) * (g1 - g3));
+  v -= (g2 + w) * (g2 + w) * (g2 + w) * lr(g2 + w, g1 + w) / (6.0L * (g0 - g2) * ((g1 - g2) * (g1 - g2)) * (g2 - g3));
+  v += (g3 + w) * (g3 + w) * (g3 + w) * lr(g3 + w, g1 + w) / (6.0L * (g0 - g3) * ((g1 - g3) * (g1 - g3)) * (g2 - g3));
+  v += (g0 + w) * (g0 + w) * (g0 + w) * lr(g0 + w, g1 + w) / (6.0L * ((g0 - g1) * (g0 - g1)) * (g0 - g2) * (g0 - g3));
+  return v;
+}
+static C s1(C g0, C g1, C g2, C g3, C w) {
+  C L10 = lr(g1 + w, g0 + w), L20 = lr(g2 + w, g0 + w), L30 = lr(g3 + w, g0 + w);
+  C v = (-(g1 + w) * (g1 + w) * L10) / ((g0 - g2) * (g0 - g3) * (g0 - g1)) * 0.5L;
+  v -= ((g1 + w) * (g1 + w) * L10 - (g2 + w) * (g2 + w) * L20) / ((g0 - g2) * (g1 - g2) * (g2 - g3)) * 0.5L;
+  v += ((g1 + w) * (g1 + w) * L10 - (g3 + w) * (g3 + w) * L30) / ((g1 - g3) * (g0 - g3) * (g2 - g3)) * 0.5L;
+  return v;
+}
 // tetra_series_vertex2 (one vertex, both signs, the kernel's form) against
-// tetra_series_weights (all four vertices, one sign) on random points
+// tetra_series_weights (all four vertices, one sign) on random points, and on
+// near-resonant normal tetrahedra against the closed forms in long double
 int main() {
   std::mt19937_64 rng(777);
   std::uniform_real_distribution<double> U(0.0, 1.0);
@@ -137,8 +158,11 @@ int main() {
     if (U(rng) < 0.2) gr[1] = gr[0];                 // averaged (degenerate) points
     if (U(rng) < 0.1) gr[3] = gr[2] = gr[0];
     const bool imag = U(rng) < 0.5;
-    const double wm = 1.5 * U(rng), wr = imag ? 0.0 : wm, wi = imag ? wm : 0.0;
+    double wm = 1.5 * U(rng), wr = imag ? 0.0 : wm, wi = imag ? wm : 0.0;
     const double mean = 0.25 * ((gr[0] + gr[1]) + (gr[2] + gr[3]));
+    // a quarter of the cases near resonance: |w + gbar| of order delt, where
+    // the unscaled powers of 1/z would overflow FP32
+    if (!imag && U(rng) < 0.25) wr = -mean + (2.0 * U(rng) - 1.0) * 0.02;
     float d[4], dmax = 0.f;
     for (int v = 0; v < 4; v++) { d[v] = (float)(gr[v] - mean); dmax = std::fmax(dmax, std::fabs(d[v])); }
     for (int pos = 0; pos < 4; pos++) {
@@ -158,7 +182,40 @@ int main() {
       }
     }
   }
-  std::printf("%ld %ld %ld %.3e\n", n, n_ok, n_mismatch_flag, worst);
+  // near resonance (|w + gbar| a few delt, r up to 1/2: up to 25 terms of
+  // (1/z)^n with |z| ~ delt) against the long-double closed forms
+  long nonfinite = 0, n_res = 0;
+  double worst_res = 0;
+  for (int it = 0; it < 20000; it++) {
+    double gr[4];
+    const double c = -1.0 + 2.0 * U(rng);
+    for (int v = 0; v < 4; v++) gr[v] = c + 0.004 * v + 0.003 * U(rng);  // separated: the normal forms apply
+    const double mean = 0.25 * ((gr[0] + gr[1]) + (gr[2] + gr[3]));
+    const double wr = -mean + (2.0 * U(rng) - 1.0) * 0.03;
+    float d[4], dmax = 0.f;
+    for (int v = 0; v < 4; v++) { d[v] = (float)(gr[v] - mean); dmax = std::fmax(dmax, std::fabs(d[v])); }
+    C g[4], w(wr, 0.0L);
+    for (int v = 0; v < 4; v++) g[v] = C(gr[v], delt);
+    C ref[4];
+    ref[0] = s2(g[1], g[0], g[2], g[3], w);
+    ref[1] = s2(g[0], g[1], g[2], g[3], w);
+    ref[2] = s2(g[0], g[2], g[1], g[3], w);
+    ref[3] = s1(g[0], g[3], g[1], g[2], w) - ref[2] - ref[1] - ref[0];
+    long double den = 0;
+    for (int v = 0; v < 4; v++) den = std::max(den, std::abs(ref[v]));
+    for (int pos = 0; pos < 4; pos++) {
+      bool ok[2];
+      rp::TsCplx x2[2];
+      rp::tetra_series_vertex2(d, d[pos], dmax, mean, delt, wr, 0.0, ok, x2);
+      for (int s2i = 0; s2i < 2; s2i++)
+        if (!std::isfinite(x2[s2i].r) || !std::isfinite(x2[s2i].i)) nonfinite++;
+      if (!ok[0]) continue;
+      n_res++;
+      const double e = (double)(std::abs(C(x2[0].r, x2[0].i) - ref[pos]) / den);
+      if (e > worst_res) worst_res = e;
+    }
+  }
+  std::printf("%ld %ld %ld %.3e %ld %ld %.3e\n", n, n_ok, n_mismatch_flag, worst, nonfinite, n_res, worst_res);
   return 0;
 }
 """
@@ -175,10 +232,14 @@ def test_vertex_series_both_signs_matches_four_vertex_form(tmp_path):
                        capture_output=True, text=True)
     if r.returncode != 0:
         pytest.fail(r.stderr)
-    n, n_ok, n_flag, worst = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
-    n, n_ok, n_flag, worst = int(n), int(n_ok), int(n_flag), float(worst)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
+    n, n_ok, n_flag, worst, nonfinite, n_res, worst_res = (int(out[0]), int(out[1]), int(out[2]), float(out[3]),
+                                                           int(out[4]), int(out[5]), float(out[6]))
+    print(f"near resonance: {n_res} vertex weights on the series, worst {worst_res:.2e} of the closed forms")
     print(f"{n_ok}/{n} on the series, {n_flag} decided differently, worst difference {worst:.2e}")
     # the r <= 1/2 test is the same up to rounding at the boundary
     assert n_flag < 1e-4 * n
     assert n_ok > 0.5 * n
     assert worst < 2e-6
+    assert nonfinite == 0
+    assert n_res > 1000 and worst_res < 2e-6
