@@ -205,9 +205,14 @@ static void tail_apply(rp_ctx *c, const rp::QTask &t, DevBuf &chi, int nen, int 
   if (!c->tail) return;
   const int ng = t.ng, ns = c->tail_nshell;
   std::vector<int> ok, sh(ng, -1);
-  for (int g = 0; g < ng; g++)
+  std::vector<double> key(ng);
+  for (int g = 0; g < ng; g++) {
     if (t.qglen[g] > 0) ok.push_back(g);
-  std::stable_sort(ok.begin(), ok.end(), [&](int a, int b) { return t.qglen[a] < t.qglen[b]; });
+    // |q+G| rounded to 2^-30 (to nearest even, as numpy's rint): lengths equal by
+    // symmetry tie, and ties keep the G order, as respackdev_gb300.tail.shells
+    key[g] = std::nearbyint(t.qglen[g] * 1073741824.0);
+  }
+  std::stable_sort(ok.begin(), ok.end(), [&](int a, int b) { return key[a] < key[b]; });
   const long n = (long)ok.size();
   for (long i = 0; i < n; i++) sh[ok[i]] = (int)std::min<long>((i * ns) / std::max<long>(n, 1), ns - 1);
   cudaStream_t st = c->st;

@@ -650,18 +650,20 @@ __global__ void __launch_bounds__(256) tetra_weights_kernel(TetraArgs a, int nec
 //
 // Every tetrahedron is classified once, as the reference's calc() does (chk1:
 // normal, or near-degenerate with some vertices replaced by their average,
-// m_tetrahedron_20170325.F:209-302, 457-503), and its points' mean (FP64) and
-// deviations (FP32) go to shared memory.  Then one thread per (mesh slot,
-// frequency) walks the tetrahedra that touch the slot (24 on a cubic mesh) and
-// sums its vertex's weight over them and both signs in FP64 registers: no
-// atomics, one fixed summation order.  The weight is the
-// confluent divided difference of the tetrahedron's (averaged) points -- the
-// quantity the reference's closed forms (:304-451) evaluate -- and for each
-// (tetrahedron, sign, frequency) where the series does not converge (r > 1/2,
-// near resonance: the Lindhard denominators of near-degenerate band pairs)
-// the reference's closed forms run in FP64 instead.  Tetrahedra cut by the
-// Fermi level take ttct and the closed forms in FP64 (other_tetra) with
-// shared-memory sums; they exist only when a band is partially occupied.
+// m_tetrahedron_20170325.F:209-302, 457-503), and its points' mean (a float
+// pair) and deviations (FP32) go to shared memory.  Then one thread per (mesh
+// slot, frequency) walks the tetrahedra that touch the slot (24 on a cubic
+// mesh) and sums its vertex's weight over them and both signs in float pairs:
+// no FP64 and no atomics in the hot loop, one fixed summation order.  The
+// weight is the confluent divided difference of the tetrahedron's (averaged)
+// points -- the quantity the reference's closed forms (:304-451) evaluate.
+// For each (tetrahedron, sign, frequency) where the series does not converge
+// (r > 1/2, near resonance: the Lindhard denominators of near-degenerate band
+// pairs) a second pass, over a compacted list, runs the reference's closed
+// forms in FP64 once for all four vertices and adds them to the outputs with
+// FP64 atomics.  Tetrahedra cut by the Fermi level take ttct and the closed
+// forms in FP64 (other_tetra) with shared-memory sums; they exist only when a
+// band is partially occupied.
 
 // A tetrahedron's code: its category in the low byte, then for each vertex
 // position (2 bits each) the position whose point it takes -- the first member
@@ -697,10 +699,10 @@ __device__ __forceinline__ void tetra_points(unsigned code, const double (&gr)[4
   }
 }
 
-// vertex pos of tetrahedron t by the reference's closed forms for one sign
-// (fk = dsgn) at frequency w, FP64
-__device__ __noinline__ double2 closed_form_vertex(const TetraArgs &a, int t, const double *e1m, const double *e2m,
-                                                   double dsgn, double wr, double wi, int pos) {
+// all four vertex weights of tetrahedron t by the reference's closed forms for
+// one sign (fk = dsgn) at frequency w, FP64
+__device__ __noinline__ bool closed_form_tetra(const TetraArgs &a, int t, const double *e1m, const double *e2m,
+                                               double dsgn, double wr, double wi, cx (&x)[4]) {
   cx ffk[4], ggk[4];
   for (int v = 0; v < 4; v++) {
     const int sl = a.imt1[4 * t + v];
@@ -708,14 +710,28 @@ __device__ __noinline__ double2 closed_form_vertex(const TetraArgs &a, int t, co
     ggk[v] = cx(-(e2m[sl] - e1m[sl]), a.delt) * dsgn;
   }
   const Chk c = chk1(a.dmna, a.dmnr, ggk);
-  cx x[4];
-  if (!calc_w(c, ffk, ggk, cx(wr, wi), x)) {
-    atomicExch(a.err, 2);
-    return make_double2(0.0, 0.0);
-  }
-  const cx r = pos == 0 ? x[0] : pos == 1 ? x[1] : pos == 2 ? x[2] : x[3];
-  return make_double2(r.r, r.i);
+  return calc_w(c, ffk, ggk, cx(wr, wi), x);
 }
+
+// (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK of mesh slot m
+__device__ __forceinline__ double2 occ_factor(const TetraArgs &a, int m, int bo, int bv) {
+  const int k = a.index_kpt[m];
+  const double2 po = a.prob[(size_t)k * a.ntb + bo], pv = a.prob[(size_t)a.kpq[k] * a.ntb + bv];
+  const double s = 1.0 / (double)a.ntk;
+  return make_double2((1.0 - (po.x * pv.x - po.y * pv.y)) * s, -(po.x * pv.y + po.y * pv.x) * s);
+}
+
+// s += v for a float pair s = (h, l) (TwoSum of the heads, tails summed)
+__device__ __forceinline__ void pair_acc(float &h, float &l, float v) {
+  const float t = h + v;
+  const float bp = t - h;
+  l += (h - (t - bp)) + (v - bp);
+  h = t;
+}
+
+// the fallback list of one pass: entries 2 * item + sign, items (e, t) with
+// item = e * ntet + t
+#define TS_FB_CAP 4096
 
 // two CTAs per SM: the smem of a 512-k mesh allows two, and the register cap
 // leaves the hot gather loop unspilled
@@ -725,15 +741,18 @@ __global__ void __launch_bounds__(256, 2) tetra_series_kernel(TetraArgs a, int n
   const int ne = min(nec, a.nen - e0);
   const int ntet = 6 * ntk;
   // per tetrahedron: the FP32 deviations d of its points from their mean, the
-  // mean (FP64) and the code; per slot the pair's energies; for metals the
-  // sums of the cut tetrahedra and their list
+  // mean as a float pair and the code; per slot the pair's energies; per
+  // frequency w as float pairs; the fallback list; for metals the sums of the
+  // cut tetrahedra and their list
   float4 *td = (float4 *)smem;
-  double *tmean = (double *)(td + ntet);
-  double *e1m = tmean + ntet, *e2m = e1m + ntk;
-  double2 *xo = (double2 *)(e2m + ntk);
+  float2 *tm = (float2 *)(td + ntet);
+  double *e1m = (double *)(tm + ntet), *e2m = e1m + ntk;
+  float4 *wsp = (float4 *)(e2m + ntk);
+  double2 *xo = (double2 *)(wsp + nec);
   int *olist = (int *)(xo + (a.may_cut ? (size_t)ntk * nec : 0));
-  unsigned short *tcode = (unsigned short *)(olist + (a.may_cut ? 2 * (size_t)ntet : 0));
-  __shared__ int ncut;
+  int *fbl = olist + (a.may_cut ? 2 * (size_t)ntet : 0);
+  unsigned short *tcode = (unsigned short *)(fbl + TS_FB_CAP);
+  __shared__ int ncut, nfb;
   const int bv = a.pair_vir[p], bo = a.pair_occ[p];
   if (threadIdx.x == 0) ncut = 0;
   for (int m = threadIdx.x; m < ntk; m += blockDim.x) {
@@ -741,10 +760,19 @@ __global__ void __launch_bounds__(256, 2) tetra_series_kernel(TetraArgs a, int n
     e1m[m] = (double)(float)a.energy[(size_t)a.numirr[k] * a.ntb + bo];
     e2m[m] = (double)(float)a.energy[(size_t)a.numirr[a.kpq[k]] * a.ntb + bv];
   }
+  for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const double2 w = a.em[e0 + e];
+    float4 f;
+    ts_split(w.x, f.x, f.y);
+    ts_split(w.y, f.z, f.w);
+    wsp[e] = f;
+  }
   if (a.may_cut)
     for (int i = threadIdx.x; i < ntk * nec; i += blockDim.x) xo[i] = make_double2(0, 0);
   __syncthreads();
   const double f = a.efermi, delt = a.delt;
+  float dh, dl;
+  ts_split(delt, dh, dl);
   // classify every tetrahedron (chk1 sees |g_a - g_b| and |g_a + g_b|, which the
   // sign does not change, so one test covers both signs) and keep its points
   for (int t = threadIdx.x; t < ntet; t += blockDim.x) {
@@ -771,7 +799,9 @@ __global__ void __launch_bounds__(256, 2) tetra_series_kernel(TetraArgs a, int n
         double gp[4];
         tetra_points(code, gr, gp);
         const double mean = 0.25 * ((gp[0] + gp[1]) + (gp[2] + gp[3]));
-        tmean[t] = mean;
+        float2 mp;
+        ts_split(mean, mp.x, mp.y);
+        tm[t] = mp;
         td[t] = make_float4((float)(gp[0] - mean), (float)(gp[1] - mean), (float)(gp[2] - mean), (float)(gp[3] - mean));
       }
     }
@@ -792,45 +822,79 @@ __global__ void __launch_bounds__(256, 2) tetra_series_kernel(TetraArgs a, int n
     __syncthreads();
   }
   // one thread per (slot, frequency): the slot's vertex weight summed over the
-  // tetrahedra around it and both signs
+  // tetrahedra around it and both signs, in FP32 with float-pair sums
   for (int it = threadIdx.x; it < ntk * ne; it += blockDim.x) {
     const int m = it % ntk, e = it / ntk;
-    const double2 w = a.em[e0 + e];
-    double ar = 0.0, ai = 0.0;
+    const float4 w = wsp[e];
+    float arh = 0.f, arl = 0.f, aih = 0.f, ail = 0.f;
     const int j1 = __ldg(a.inc_off + m + 1);
     for (int j = __ldg(a.inc_off + m); j < j1; j++) {
       const int ent = __ldg(a.inc + j), t = ent >> 2, pos = ent & 3;
       const int cat = tcode[t] & 0xff;
       if (cat == TC_SKIP || cat == TC_OTHER) continue;
       const float4 d4 = td[t];
+      const float2 mp = tm[t];
       const float d[4] = {d4.x, d4.y, d4.z, d4.w};
       const float dmax = fmaxf(fmaxf(fabsf(d4.x), fabsf(d4.y)), fmaxf(fabsf(d4.z), fabsf(d4.w)));
       const float dv = pos == 0 ? d4.x : pos == 1 ? d4.y : pos == 2 ? d4.z : d4.w;
+      float zr[2], zi[2], inv[2];
       bool ok[2];
+      ts_z(w.x, w.y, w.z, w.w, mp.x, mp.y, dh, dl, dmax, zr, zi, ok, inv);
       TsCplx x[2];
-      tetra_series_vertex2(d, dv, dmax, tmean[t], delt, w.x, w.y, ok, x);
+      tetra_series_core(d, dv, dmax, zr, zi, ok, inv, x);
       // fk = dsgn: the sign -1 enters negated
-      ar += (double)x[0].r - (double)x[1].r;
-      ai += (double)x[0].i - (double)x[1].i;
-      if (!ok[0]) {
-        const double2 c = closed_form_vertex(a, t, e1m, e2m, 1.0, w.x, w.y, pos);
-        ar += c.x;
-        ai += c.y;
+      pair_acc(arh, arl, x[0].r - x[1].r);
+      pair_acc(aih, ail, x[0].i - x[1].i);
+    }
+    const int k = a.index_kpt[m];
+    const double2 pp = occ_factor(a, m, bo, bv);
+    double2 x = make_double2((double)arh + (double)arl, (double)aih + (double)ail);
+    if (a.may_cut) x = cadd(x, xo[(size_t)m * nec + e]);
+    // w[(p*nen + e)*ntk + k] = xow(m, e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
+    wout[((size_t)p * a.nen + e0 + e) * ntk + k] = cmul(x, pp);
+  }
+  __syncthreads();
+  // the (tetrahedron, sign, frequency) where the series was not taken (the same
+  // decision, from the same float inputs): the closed forms in FP64 for all
+  // four vertices at once, added to the CTA's own outputs
+  const int nitem = ntet * ne;
+  for (int base = 0; base < nitem; base += TS_FB_CAP / 2) {
+    if (threadIdx.x == 0) nfb = 0;
+    __syncthreads();
+    const int iend = min(nitem, base + TS_FB_CAP / 2);
+    for (int i = base + threadIdx.x; i < iend; i += blockDim.x) {
+      const int t = i % ntet, e = i / ntet;
+      const int cat = tcode[t] & 0xff;
+      if (cat == TC_SKIP || cat == TC_OTHER) continue;
+      const float4 d4 = td[t];
+      const float2 mp = tm[t];
+      const float4 w = wsp[e];
+      const float dmax = fmaxf(fmaxf(fabsf(d4.x), fabsf(d4.y)), fmaxf(fabsf(d4.z), fabsf(d4.w)));
+      float zr[2], zi[2], inv[2];
+      bool ok[2];
+      ts_z(w.x, w.y, w.z, w.w, mp.x, mp.y, dh, dl, dmax, zr, zi, ok, inv);
+      for (int sg = 0; sg < 2; sg++)
+        if (!ok[sg]) fbl[atomicAdd(&nfb, 1)] = 2 * i + sg;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < nfb; j += blockDim.x) {
+      const int ent = fbl[j], i = ent >> 1, sg = ent & 1;
+      const int t = i % ntet, e = i / ntet;
+      const double2 w = a.em[e0 + e];
+      cx x[4];
+      if (!closed_form_tetra(a, t, e1m, e2m, sg ? -1.0 : 1.0, w.x, w.y, x)) {
+        atomicExch(a.err, 2);
+        continue;
       }
-      if (!ok[1]) {
-        const double2 c = closed_form_vertex(a, t, e1m, e2m, -1.0, w.x, w.y, pos);
-        ar += c.x;
-        ai += c.y;
+      for (int v = 0; v < 4; v++) {
+        const int m = a.imt1[4 * t + v];
+        const double2 r = cmul(make_double2(x[v].r, x[v].i), occ_factor(a, m, bo, bv));
+        double2 *o = wout + ((size_t)p * a.nen + e0 + e) * ntk + a.index_kpt[m];
+        atomicAdd(&o->x, r.x);
+        atomicAdd(&o->y, r.y);
       }
     }
-    // w[(p*nen + e)*ntk + k] = xow(m, e) * (1 - P_occ(bo,k) P_vir(bv,k+q)) / NTK
-    const int k = a.index_kpt[m];
-    const double2 po = a.prob[(size_t)k * a.ntb + bo], pv = a.prob[(size_t)a.kpq[k] * a.ntb + bv];
-    const double2 pp = make_double2(1.0 - (po.x * pv.x - po.y * pv.y), -(po.x * pv.y + po.y * pv.x));
-    double2 x = make_double2(ar, ai);
-    if (a.may_cut) x = cadd(x, xo[(size_t)m * nec + e]);
-    const double2 r = cmul(x, pp);
-    wout[((size_t)p * a.nen + e0 + e) * ntk + k] = make_double2(r.x / (double)ntk, r.y / (double)ntk);
+    __syncthreads();
   }
 }
 
@@ -838,12 +902,13 @@ int launch_tetra_weights(const TetraArgs &a, double2 *w, cudaStream_t st, bool s
   if (a.npair == 0) return 0;
   if (series) {
     if (!a.inc_off || !a.inc) fail(1, "tetrahedron series kernel: no vertex incidence lists");
-    // the tetrahedra's points and codes, e1m and e2m, plus for metals the
-    // cut-tetrahedron list and the sums of a frequency chunk
+    // the tetrahedra's deviations, means and codes, e1m and e2m, the fallback
+    // list, plus for metals the cut-tetrahedron list and the sums of a
+    // frequency chunk; per frequency its float pairs
     const size_t ntk = (size_t)a.ntk, ntet = 6 * ntk;
-    const size_t fixed = (sizeof(float4) + sizeof(double) + sizeof(unsigned short)) * ntet + 2 * sizeof(double) * ntk +
-                         (a.may_cut ? 2 * sizeof(int) * ntet : 0);
-    const size_t per_e = a.may_cut ? sizeof(double2) * ntk : 0;
+    const size_t fixed = (sizeof(float4) + sizeof(float2) + sizeof(unsigned short)) * ntet + 2 * sizeof(double) * ntk +
+                         sizeof(int) * TS_FB_CAP + (a.may_cut ? 2 * sizeof(int) * ntet : 0);
+    const size_t per_e = sizeof(float4) + (a.may_cut ? sizeof(double2) * ntk : 0);
     int nec = a.nen;
     while (nec > 1 && fixed + per_e * nec > 210 * 1024) nec--;
     const size_t smem = fixed + per_e * nec;

@@ -109,34 +109,52 @@ static const float kTsA[TS_NMAX] = {RP_TS_A5(0), RP_TS_A5(5), RP_TS_A5(10), RP_T
                                     RP_TS_A5(25)};
 #endif
 
-// The weight of one vertex for both signs at once.  d[i] = g_i - gbar (FP32)
-// for the sign +1, with g_i the tetrahedron's points (near-degenerate vertices
-// already replaced by their average, as the reference's calc() does) and gbar
-// = mean their mean (double); dv = d of the vertex; dmax = max |d|.  The sign
-// -1 negates every d, so it shares the h_n and its terms carry (-1)^n; its z
-// is w - gbar - i delt.  ok[s] says whether the series was taken for sign s
-// (s = 0: +1, s = 1: -1): false where r > TS_RMAX or z = 0, x[s] then 0.
-// Values in the closed forms' normalisation (before the factor fk = dsgn).
+// Products and sums that the compiler must not contract into FMAs, so that
+// every caller that decides whether the series is taken for a (tetrahedron,
+// sign, frequency) decides the same way.
+#if defined(__CUDA_ARCH__)
+#define RP_TS_MUL(a, b) __fmul_rn((a), (b))
+#define RP_TS_ADD(a, b) __fadd_rn((a), (b))
+#else
+#define RP_TS_MUL(a, b) ((a) * (b))
+#define RP_TS_ADD(a, b) ((a) + (b))
+#endif
+
+// (ah + al) + (bh + bl) for two float pairs, rounded once to float: TwoSum of
+// the heads, then the tails (z = w + gbar to about one rounding, without FP64)
+RP_TS_HD float ts_pair_sum(float ah, float al, float bh, float bl) {
+  const float s = RP_TS_ADD(ah, bh);
+  const float bp = RP_TS_ADD(s, -ah);
+  const float err = RP_TS_ADD(RP_TS_ADD(ah, -RP_TS_ADD(s, -bp)), RP_TS_ADD(bh, -bp));
+  return RP_TS_ADD(s, RP_TS_ADD(err, RP_TS_ADD(al, bl)));
+}
+
+// Whether the series is taken at z (r = dmax / |z| <= TS_RMAX, z != 0), and 1 / |z|^2.
+RP_TS_HD void ts_decide(float zr, float zi, float dmax, bool &ok, float &inv) {
+  const float zz = RP_TS_ADD(RP_TS_MUL(zr, zr), RP_TS_MUL(zi, zi));
+  ok = zz > 0.f && RP_TS_MUL(dmax, dmax) <= RP_TS_MUL(TS_RMAX * TS_RMAX, zz);
+  inv = ok ? 1.f / zz : 0.f;
+}
+
+// The weight of one vertex for both signs at once, given each sign's z and
+// decision (ts_decide).  d[i] = g_i - gbar (FP32) for the sign +1, with g_i the
+// tetrahedron's points (near-degenerate vertices already replaced by their
+// average, as the reference's calc() does) and gbar their mean; dv = d of the
+// vertex; dmax = max |d|.  The sign -1 negates every d, so it shares the h_n
+// and its terms carry (-1)^n.  x[s] = 0 where ok[s] is false.  Values in the
+// closed forms' normalisation (before the factor fk = dsgn).
 //
 // Near resonance |z| is of order delt and u^n alone would overflow FP32 (and
 // h_n underflow) long before their product, which r^n bounds, is small.  So
 // with sc = 1/min|z| over the signs taken, the recurrences run on d sc
 // (|d sc| <= r) and u / sc (|u / sc| <= 1): h_n(d) u^n = h_n(d sc) (u / sc)^n.
-RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, double mean, double delt, double wr,
-                                   double wi, bool (&ok)[2], TsCplx (&x)[2]) {
-  float zr[2], zi[2], inv[2], sc = 0.f;
-  for (int s = 0; s < 2; s++) {
-    const double sg = s == 0 ? 1.0 : -1.0;
-    // z in double (one subtraction's worth of care), the rest in FP32
-    zr[s] = (float)(wr + sg * mean);
-    zi[s] = (float)(wi + sg * delt);
-    const float zz = zr[s] * zr[s] + zi[s] * zi[s];
-    ok[s] = zz > 0.f && dmax * dmax <= TS_RMAX * TS_RMAX * zz;
-    inv[s] = ok[s] ? 1.f / zz : 0.f;
-    if (ok[s]) sc = fmaxf(sc, sqrtf(inv[s]));
-    x[s] = TsCplx{0.f, 0.f};
-  }
+RP_TS_HD void tetra_series_core(const float (&d)[4], float dv, float dmax, const float (&zr)[2], const float (&zi)[2],
+                                const bool (&ok)[2], const float (&inv)[2], TsCplx (&x)[2]) {
+  x[0] = x[1] = TsCplx{0.f, 0.f};
   if (!ok[0] && !ok[1]) return;
+  float sc = 0.f;
+  for (int s = 0; s < 2; s++)
+    if (ok[s]) sc = fmaxf(sc, sqrtf(inv[s]));
   // scaled u = conj(z) / |z|^2 / sc of each sign, and the scaled deviations
   const float is = 1.f / sc;
   const float ur0 = zr[0] * inv[0] * is, ui0 = -zi[0] * inv[0] * is;
@@ -181,6 +199,38 @@ RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, do
     const float ar = zr[1] * inv[1], ai = -zi[1] * inv[1];
     x[1] = TsCplx{ar * sr1 - ai * si1, ar * si1 + ai * sr1};
   }
+}
+
+// a double as a float pair (hi + lo to about 2^-48 relative)
+RP_TS_HD void ts_split(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// z_s = w + s (gbar + i delt) of sign s (s = 0: +1, s = 1: -1) from float pairs,
+// and its decision: the one formation the gather and the fallback pass share.
+RP_TS_HD void ts_z(float wrh, float wrl, float wih, float wil, float mh, float ml, float dh, float dl, float dmax,
+                   float (&zr)[2], float (&zi)[2], bool (&ok)[2], float (&inv)[2]) {
+  zr[0] = ts_pair_sum(wrh, wrl, mh, ml);
+  zi[0] = ts_pair_sum(wih, wil, dh, dl);
+  zr[1] = ts_pair_sum(wrh, wrl, -mh, -ml);
+  zi[1] = ts_pair_sum(wih, wil, -dh, -dl);
+  ts_decide(zr[0], zi[0], dmax, ok[0], inv[0]);
+  ts_decide(zr[1], zi[1], dmax, ok[1], inv[1]);
+}
+
+// The same from double inputs (the host tests' interface), with z formed as
+// the device forms it.  ok[s] says whether the series was taken for sign s.
+RP_TS_HD void tetra_series_vertex2(const float (&d)[4], float dv, float dmax, double mean, double delt, double wr,
+                                   double wi, bool (&ok)[2], TsCplx (&x)[2]) {
+  float wrh, wrl, wih, wil, mh, ml, dh, dl;
+  ts_split(wr, wrh, wrl);
+  ts_split(wi, wih, wil);
+  ts_split(mean, mh, ml);
+  ts_split(delt, dh, dl);
+  float zr[2], zi[2], inv[2];
+  ts_z(wrh, wrl, wih, wil, mh, ml, dh, dl, dmax, zr, zi, ok, inv);
+  tetra_series_core(d, dv, dmax, zr, zi, ok, inv, x);
 }
 
 }  // namespace rp

