@@ -65,7 +65,10 @@ typedef struct rp_params {
   int    pair_batch;           /* at most this many band pairs per batch of a
                                   q (0 = as many as fit in 24 GB)             */
   int    tc_split;             /* K splits of the tensor-core Gram launch (0 =
-                                  measured per shape by the split tuner)      */
+                                  measured per shape by the launch tuner)     */
+  int    tc_pair;              /* tensor-core Gram CTAs: 1 single CTAs, 2 CTA
+                                  pairs (cta_group::2), 0 measured per shape
+                                  by the launch tuner                         */
   int    write_eps_f32;        /* 1: rp_write_q also writes dat.epsqw.c4, the
                                   complex(4) eps^-1 calc_int reads (Gamma: the
                                   mean of the three directions)              */

@@ -35,7 +35,7 @@ class Params(C.Structure):
         ("n_calc_q", C.c_int), ("mpi_num_qcomm", C.c_int), ("precision", C.c_int), ("fft_box", C.c_int * 3),
         ("dump_chi", C.c_int), ("device", C.c_int), ("max_pairs", C.c_int), ("qshard_index", C.c_int),
         ("qshard_count", C.c_int), ("pair_fp64", C.c_int), ("tc_ksub", C.c_int),
-        ("pair_batch", C.c_int), ("tc_split", C.c_int), ("write_eps_f32", C.c_int), ("eps_fp64", C.c_int),
+        ("pair_batch", C.c_int), ("tc_split", C.c_int), ("tc_pair", C.c_int), ("write_eps_f32", C.c_int), ("eps_fp64", C.c_int),
         ("tetra_fp64", C.c_int), ("ur_window", C.c_int), ("tail_model", C.c_char * 256),
     ]
 

@@ -630,6 +630,7 @@ static void chi0_q(rp_ctx *c, int iq, bool fast) {
   RP_CUDA(cudaEventRecord(c->ev[5], c->st));
   if (fast) {
     c->tcw.ksub = S.params.tc_ksub;
+    c->tcw.pair_req = S.params.tc_pair;
     rp::tc_begin_q(c->tcw, r.ng, r.nen, r.ndir, S.params.tc_split, (long)r.npair * r.ntk, S.params.precision, c->st);
   }
   for (int bi = 0; bi < q_nbatch(r); bi++) q_batch(c, r, bi, &c->tcw, true);
@@ -916,6 +917,7 @@ int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, dou
           for (int bi = 0; bi < q_nbatch(p.r); bi++) {
             auto ws = std::make_unique<rp::TcWorkspace>();
             ws->ksub = c->S.params.tc_ksub;
+            ws->pair_req = c->S.params.tc_pair;
             rp::tc_begin_q(*ws, p.r.ng, p.r.nen, p.r.ndir, c->S.params.tc_split,
                            (long)q_batch_pairs(p.r, bi) * p.r.ntk, prec, c->st);
             p.ws.push_back(std::move(ws));

@@ -288,6 +288,7 @@ void parse_namelist_text(const std::string &text, rp_params *p, std::vector<int>
       else if (k == "tc_ksub") p->tc_ksub = nl_int(v, k);
       else if (k == "pair_batch") p->pair_batch = nl_int(v, k);
       else if (k == "tc_split") p->tc_split = nl_int(v, k);
+      else if (k == "tc_pair") p->tc_pair = nl_int(v, k);
       else if (k == "write_eps_f32") p->write_eps_f32 = nl_int(v, k);
       else if (k == "eps_fp64") p->eps_fp64 = nl_int(v, k);
       else if (k == "ur_window") p->ur_window = nl_int(v, k);

@@ -116,14 +116,56 @@ __device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// try_wait with cluster-scope acquire: for barriers the peer CTA of a pair arrives on
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t *b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// the shared::cluster address of a local shared variable's copy in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_bar) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_bar) : "memory");
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// The CTA's abort flag; in a CTA pair raising it also raises the peer's, so
+// both halves of the pair leave their waits.
+struct Abort {
+  volatile int *flag;
+  uint32_t peer;  // the peer's flag (shared::cluster address), 0 without a pair
+  __device__ __forceinline__ bool up() const { return *flag != 0; }
+  __device__ __forceinline__ void raise() const {
+    *flag = 1;
+    if (peer) asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(peer), "r"(1) : "memory");
+  }
+};
+
 // bounded wait; returns false (and raises the abort flag) when it gives up
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag) {
+template <bool CLUSTER = false>
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, const Abort &ab) {
   for (long i = 0; i < WAIT_LIMIT; i++) {
-    if (mbar_try(b, parity)) return true;
-    if (*abort_flag) return false;
+    if (CLUSTER ? mbar_try_cluster(b, parity) : mbar_try(b, parity)) return true;
+    if (ab.up()) return false;
     if (i > 64) __nanosleep(32);
   }
-  *abort_flag = 1;
+  ab.raise();
   return false;
 }
 
@@ -150,37 +192,49 @@ __host__ __device__ constexpr uint32_t make_idesc(int bf16, int M, int N) {
 // COLL: the A operand's collector buffer -- 0 not kept, 1 fill (read A, keep
 // it), 2 use (the kept A, keep it), 3 last use (the kept A, release it).  The
 // products that share an A plane run back to back, so that plane is read from
-// shared memory once per K step instead of once per product.
-template <int COLL>
+// shared memory once per K step instead of once per product.  CG: 1 one CTA
+// (128 x N), 2 a CTA pair (256 x N: each CTA its 128 rows of A, N/2 rows of B
+// and its 128 rows of D), issued by the pair's first CTA.
+#define RP_MMA_F16(CGS, COLLS)                                                                    \
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"                                 \
+               "tcgen05.mma.cta_group::" CGS ".kind::f16" COLLS " [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem), \
+               "l"(ad), "l"(bd), "r"(idesc), "r"(accum))
+template <int COLL, int CG>
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
-  if (COLL == 1)
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
-  else if (COLL == 2)
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::use [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
-  else if (COLL == 3)
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
-  else
-    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
-                 "l"(ad), "l"(bd), "r"(idesc), "r"(accum));
+  if (CG == 1) {
+    if (COLL == 1) RP_MMA_F16("1", ".collector::a::fill");
+    else if (COLL == 2) RP_MMA_F16("1", ".collector::a::use");
+    else if (COLL == 3) RP_MMA_F16("1", ".collector::a::lastuse");
+    else RP_MMA_F16("1", "");
+  } else {
+    if (COLL == 1) RP_MMA_F16("2", ".collector::a::fill");
+    else if (COLL == 2) RP_MMA_F16("2", ".collector::a::use");
+    else if (COLL == 3) RP_MMA_F16("2", ".collector::a::lastuse");
+    else RP_MMA_F16("2", "");
+  }
 }
+#undef RP_MMA_F16
 // the collector mode of product pb of an A plane that has npb products
-template <int PB, int NPB>
+template <int PB, int NPB, int CG>
 __device__ __forceinline__ void mma_plane(uint32_t dtmem, uint64_t ad, uint64_t bd, uint32_t idesc, int accum) {
-  if (NPB == 1) mma_f16<0>(dtmem, ad, bd, idesc, accum);
-  else if (PB == 0) mma_f16<1>(dtmem, ad, bd, idesc, accum);
-  else if (PB == NPB - 1) mma_f16<3>(dtmem, ad, bd, idesc, accum);
-  else mma_f16<2>(dtmem, ad, bd, idesc, accum);
+  if (NPB == 1) mma_f16<0, CG>(dtmem, ad, bd, idesc, accum);
+  else if (PB == 0) mma_f16<1, CG>(dtmem, ad, bd, idesc, accum);
+  else if (PB == NPB - 1) mma_f16<3, CG>(dtmem, ad, bd, idesc, accum);
+  else mma_f16<2, CG>(dtmem, ad, bd, idesc, accum);
 }
+// arrive on barrier b when this thread's MMAs are done: in this CTA, or (CG 2)
+// on the barrier at the same offset in both CTAs of the pair
+template <int CG>
 __device__ __forceinline__ void mma_commit(uint64_t *b) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
-               : "memory");
+  if (CG == 1)
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(b))
+                 : "memory");
+  else
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+            smem_u32(b)),
+        "h"((unsigned short)3)
+        : "memory");
 }
 
 
@@ -306,34 +360,52 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // NP operand planes, EXACT integer leading plane, BF16 or FP16.  One CTA per
 // work item (problem, upper tile, frequency, Re/Im weight, K split); see the
 // file comment for the roles.
-template <int NP, bool EXACT, bool BF16>
+//
+// PAIR: a cluster of two CTAs computes the 256 x 128 block of rows ta, ta + 1
+// (work items 2i, 2i + 1) and columns tb with tcgen05.mma.cta_group::2.  Each
+// CTA produces its own 128 A rows and bulk-copies half of the B tile (64 of
+// its 128 rows: the first or second 8 KB of each 128-byte-swizzled plane
+// tile), so a pair reads and writes a third less shared memory per product
+// than two single CTAs, and one thread issues the MMAs of both.  The first CTA
+// (rank 0) issues; its commits arrive on the barriers of both CTAs.  The
+// second CTA's MMA warp relays to the first: lane 0 that a stage of its
+// operands is ready (pready), lane 1 that its epilogue has drained an
+// accumulator buffer (paccempty).
+template <int NP, bool EXACT, bool BF16, bool PAIR>
 // 22 warps: at most 6 on one SM sub-partition, whose 16K registers allow 85 per thread
 __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   __shared__ TcArgs sh_args;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  constexpr int CG = PAIR ? 2 : 1;
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
+  constexpr int BTILE = PAIR ? TILE_BYTES / 2 : TILE_BYTES;  // this CTA's rows of a B plane tile
   constexpr int AOFF = 0, BOFF = NP * TILE_BYTES;
-  constexpr int STAGE = 2 * NP * TILE_BYTES;        // A planes, B planes
+  constexpr int STAGE = NP * TILE_BYTES + NP * BTILE;  // A planes, B planes
   unsigned char *stage_base = smem;
   unsigned char *wring = smem + (size_t)NSTAGE * STAGE;  // two weight chunks
   uint64_t *bars = (uint64_t *)(wring + 2 * WBYTES);
   uint64_t *full = bars, *bfull = bars + 2, *empty = bars + 4, *accfull = bars + 6, *accempty = bars + 8,
            *wready = bars + 10, *wfree = bars + 12, *fin = bars + 14;
-  volatile int *abort_flag = (volatile int *)(bars + 15);
+  volatile int *abort_word = (volatile int *)(bars + 15);
   uint32_t *tmem_slot = (uint32_t *)(bars + 16);
+  uint64_t *pready = bars + 18, *paccempty = bars + 20;  // the pair's relays (used in rank 0)
   float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
   float *rB_s = sA_s + BM;                          // 1 / column scales of the B tile (128)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = PAIR ? cluster_rank() : 0;
+  const Abort ab{abort_word, PAIR ? cluster_addr((const void *)abort_word, rank ^ 1u) : 0u};
   // the work list has channels fastest, so the CTAs running together share their operand rows in L2
   const int4 wk = grp.work[blockIdx.x];
   const TcArgs &a = sh_args;
   const int ta = wk.y & 0xffff, tb = wk.y >> 16;
   const int cidx = wk.z, e = cidx >> 1, ch = cidx & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
   {
+    // empty K range (the host makes none): the whole CTA leaves, and so does
+    // its peer, whose work item has the same K range
     const TcArgs &p = grp.probs[wk.x];
-    if (wk.w * p.kb_split >= p.Kp / BK) return;  // empty K range (the host makes none): the whole CTA leaves
+    if (wk.w * p.kb_split >= p.Kp / BK) return;
   }
 
   if (tid == 0) {
@@ -346,18 +418,28 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       mbar_init(&accempty[s], NEPI);
       mbar_init(&wready[s], 1);
       mbar_init(&wfree[s], NPROD);
+      mbar_init(&pready[s], 1);
+      mbar_init(&paccempty[s], 1);
     }
     mbar_init(fin, 1);
-    *abort_flag = 0;
+    *abort_word = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == MMA_WARP) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(512));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    if (PAIR) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(512));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                   "r"(512));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
   }
   tc_fence_before();
   __syncthreads();
+  // both CTAs of a pair: barriers initialised and tensor memory allocated before either uses the other's
+  if (PAIR) cluster_sync();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
   // this CTA's K range: blocks kb0 .. kb0 + nkb - 1 of the problem
@@ -396,8 +478,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
         for (int i = 0; i < PROWS; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
       }
       const int wc = kb / WCHUNK, kin = kb % WCHUNK;
-      if (kin == 0 && !mbar_wait(&wready[wc & 1], (wc >> 1) & 1, abort_flag)) break;  // this chunk's weights
-      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
+      if (kin == 0 && !mbar_wait(&wready[wc & 1], (wc >> 1) & 1, ab)) break;  // this chunk's weights
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, ab)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
       // (hi, lo) of K = 2 lane and 2 lane + 1
       const float4 wv = *(const float4 *)(wring + (size_t)(wc & 1) * WBYTES + ((size_t)kin * BK + 2 * lane) * 8);
@@ -437,7 +519,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
                   rl;  // + col * BM
     for (int sc = 0; sc < nsub; sc++) {
       const int b = sc & 1;
-      if (!mbar_wait(&accfull[b], (sc >> 1) & 1, abort_flag)) break;
+      if (!mbar_wait(&accfull[b], (sc >> 1) & 1, ab)) break;
       tc_fence_after();
       const uint32_t base = lanebase + (uint32_t)(b * NACC * BN);
       // the running sums of the next 8 columns are loaded while these 8 are
@@ -469,9 +551,27 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       mbar_arrive(&accempty[b]);
     }
   } else if (warp == MMA_WARP) {
-    if (lane == 0) {
+    if (PAIR && rank == 1) {
+      // ---------------- the second CTA of a pair: relays to the issuer ----------------
+      if (lane == 0) {
+        const uint32_t rp0 = cluster_addr(&pready[0], 0), rp1 = cluster_addr(&pready[1], 0);
+        for (int kb = 0; kb < nkb; kb++) {
+          const int s = kb & 1, use = kb >> 1;
+          if (!mbar_wait(&bfull[s], use & 1, ab) || !mbar_wait(&full[s], use & 1, ab)) break;
+          mbar_arrive_remote(s ? rp1 : rp0);
+        }
+      } else if (lane == 1) {
+        const uint32_t ra0 = cluster_addr(&paccempty[0], 0), ra1 = cluster_addr(&paccempty[1], 0);
+        // the issuer waits for the drains of sub-chunks 0 .. nsub - 3 only
+        for (int sc = 0; sc + 2 < nsub; sc++) {
+          const int b = sc & 1;
+          if (!mbar_wait(&accempty[b], (sc >> 1) & 1, ab)) break;
+          mbar_arrive_remote(b ? ra1 : ra0);
+        }
+      }
+    } else if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      const uint32_t idesc = make_idesc(BF16 ? 1 : 0, BM, BN);
+      const uint32_t idesc = make_idesc(BF16 ? 1 : 0, PAIR ? 2 * BM : BM, BN);
       // descriptors of every plane tile of both stages, built once: per MMA the
       // issuing thread only adds the K step (32 bytes = 2 units of the start
       // address), since it shares its sub-partition with busy producer warps
@@ -481,8 +581,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       for (int p = 0; p < NP; p++) {
         dA0[p] = make_desc(sb0 + (uint32_t)(AOFF + p * TILE_BYTES));
         dA1[p] = make_desc(sb0 + (uint32_t)(STAGE + AOFF + p * TILE_BYTES));
-        dB0[p] = make_desc(sb0 + (uint32_t)(BOFF + p * TILE_BYTES));
-        dB1[p] = make_desc(sb0 + (uint32_t)(STAGE + BOFF + p * TILE_BYTES));
+        dB0[p] = make_desc(sb0 + (uint32_t)(BOFF + p * BTILE));
+        dB1[p] = make_desc(sb0 + (uint32_t)(STAGE + BOFF + p * BTILE));
       }
       // the MMAs of one K block in stage S: products of planes pa (A) and pb (B)
       // with pa + pb <= NP - 1, grouped by A plane (collector reuse); with the
@@ -499,7 +599,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
             const uint64_t bd = (S == 0 ? dB0[pb] : dB1[pb]) + (uint64_t)(2 * kk);
             constexpr bool main_acc = (EXACT && pa == 0 && pb == 0) || !EXACT;
             constexpr bool first = main_acc ? (pa == 0 && pb == 0) : (pa == 0 && pb == 1);
-            mma_plane<pb, NP - pa>(main_acc ? tacc : tacc + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
+            mma_plane<pb, NP - pa, CG>(main_acc ? tacc : tacc + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
           };
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
@@ -511,35 +611,39 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
           }
         }
       };
-      for (int sc = 0; sc < nsub && !*abort_flag; sc++) {
-        // accumulator pair b; the epilogue must have drained it (sub-chunk sc - 2)
+      for (int sc = 0; sc < nsub && !ab.up(); sc++) {
+        // accumulator pair b; the epilogues must have drained it (sub-chunk sc - 2)
         const int b = sc & 1;
-        if (sc >= 2 && !mbar_wait(&accempty[b], ((sc - 2) >> 1) & 1, abort_flag)) break;
+        if (sc >= 2) {
+          if (!mbar_wait(&accempty[b], ((sc - 2) >> 1) & 1, ab)) break;
+          if (PAIR && !mbar_wait<true>(&paccempty[b], ((sc - 2) >> 1) & 1, ab)) break;
+        }
         tc_fence_after();
         const uint32_t tacc = tmem + (uint32_t)(b * NACC * BN);
         const int kbeg = sc * ksub, kend = min(nkb, kbeg + ksub);
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
           const int s = kb & 1, use = kb >> 1;
-          if (!mbar_wait(&bfull[s], use & 1, abort_flag) || !mbar_wait(&full[s], use & 1, abort_flag)) {
+          if (!mbar_wait(&bfull[s], use & 1, ab) || !mbar_wait(&full[s], use & 1, ab) ||
+              (PAIR && !mbar_wait<true>(&pready[s], use & 1, ab))) {
             ok = false;
             break;
           }
           tc_fence_after();
           if (s == 0) issue(std::integral_constant<int, 0>{}, kb == kbeg, tacc);
           else issue(std::integral_constant<int, 1>{}, kb == kbeg, tacc);
-          mma_commit(&empty[s]);
+          mma_commit<CG>(&empty[s]);
         }
         if (!ok) break;
-        mma_commit(&accfull[b]);
+        mma_commit<CG>(&accfull[b]);
       }
       // wait for every MMA this thread issued before tensor memory is released
-      mma_commit(fin);
-      mbar_wait(fin, 0, abort_flag);
+      mma_commit<CG>(fin);
+      mbar_wait(fin, 0, ab);
     }
   } else if (lane == 0) {
     // ---------------- loader: B planes per K block, weights per chunk, by bulk copy ----------------
-    const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES;
+    const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES + (size_t)rank * BTILE;
     const float2 *wsrc = a.wt + (size_t)cidx * a.Kp + (size_t)kb0 * BK;
     const int nchunk = (nkb + WCHUNK - 1) / WCHUNK;
     auto issue_w = [&](int c) {
@@ -552,23 +656,23 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     int wnext = 2, issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb & 1, use = kb >> 1;
-      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, abort_flag)) break;
+      if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, ab)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
       if (kb + PF_AHEAD < nkb) bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
-      mbar_arrive_tx(&bfull[s], (uint32_t)(NP * TILE_BYTES));
+      mbar_arrive_tx(&bfull[s], (uint32_t)(NP * BTILE));
 #pragma unroll
       for (int p = 0; p < NP; p++)
-        bulk_g2s(st + BOFF + p * TILE_BYTES, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, TILE_BYTES, &bfull[s]);
+        bulk_g2s(st + BOFF + p * BTILE, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, BTILE, &bfull[s]);
       issued = kb + 1;
       // chunk wnext reuses the slot of chunk wnext - 2 once the producers have left it
       if (wnext < nchunk && kb >= (wnext - 1) * WCHUNK) {
-        if (!mbar_wait(&wfree[wnext & 1], ((wnext - 2) >> 1) & 1, abort_flag)) break;
+        if (!mbar_wait(&wfree[wnext & 1], ((wnext - 2) >> 1) & 1, ab)) break;
         issue_w(wnext);
         wnext++;
       }
     }
     // after an abort, wait (bounded) for the copies still in flight before the CTA exits
-    if (*abort_flag) {
+    if (ab.up()) {
       for (int kb = max(0, issued - NSTAGE); kb < issued; kb++)
         for (long i = 0; i < WAIT_LIMIT && !mbar_try(&bfull[kb & 1], (kb >> 1) & 1); i++) __nanosleep(32);
       for (int c = max(0, wnext - 2); c < wnext; c++)
@@ -576,12 +680,16 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     }
   }
   __syncwarp();
-  if (tid == 0 && *abort_flag) atomicExch(grp.err, 4);
+  if (tid == 0 && ab.up()) atomicExch(grp.err, 4);
   tc_fence_before();
   __syncthreads();
+  // a pair: the issuer's MMAs (which read both CTAs' shared memory and write
+  // both CTAs' tensor memory) are complete before either CTA frees or leaves
+  if (PAIR) cluster_sync();
   if (warp == MMA_WARP) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    if (PAIR) asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    else asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
 }
 
@@ -762,10 +870,12 @@ static void *grow(void *&p, size_t &have, size_t need) {
 
 static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
 static int nplanes_of(int precision) { return (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2; }
-static size_t smem_of(int precision) {
-  // per stage: A planes, B planes; the weight ring; then the barriers and the scales
-  return 1024 + (size_t)NSTAGE * 2 * (size_t)nplanes_of(precision) * TILE_BYTES + 2 * (size_t)WBYTES + 256 +
-         2 * sizeof(float) * BM;
+static size_t smem_of(int precision, bool pair) {
+  // per stage: A planes, B planes (half a tile each in a CTA pair); the weight
+  // ring; then the barriers and the scales
+  const size_t np = (size_t)nplanes_of(precision);
+  return 1024 + (size_t)NSTAGE * np * (TILE_BYTES + (pair ? TILE_BYTES / 2 : TILE_BYTES)) + 2 * (size_t)WBYTES +
+         256 + 2 * sizeof(float) * BM;
 }
 static size_t slice_of(int Mp, int nen) { return (size_t)nen * 2 * Mp * Mp; }
 // K blocks per FP32 sub-chunk: 1024 K by default; the integer leading plane's
@@ -776,17 +886,19 @@ static int ksub_of(const TcWorkspace &ws) {
 }
 
 // ---------------------------------------------------------------------------
-// K-split tuner.  A q point whose upper tiles x channels give fewer than two
-// CTAs per SM leaves SMs idle; splitting K across CTAs (each split into its
-// own float-pair slice, summed when chi is assembled) fills them at the cost
-// of more sums to drain.  The best split of a shape (precision, Mp, nen, K
-// order of magnitude) is measured once on the first batch of that shape and
-// cached for the process.
+// Launch-shape tuner.  A q point whose upper tiles x channels give fewer than
+// two CTAs per SM leaves SMs idle; splitting K across CTAs (each split into
+// its own float-pair slice, summed when chi is assembled) fills them at the
+// cost of more sums to drain.  CTA pairs (cta_group::2) read less shared
+// memory per product but compute the row tiles below the diagonal that pair
+// with the diagonal ones.  The best (split, pair) of a shape (precision, Mp,
+// nen, K order of magnitude) is measured once on the first batch of that shape
+// and cached for the process.
 
 namespace {
 constexpr int SPLIT_MAX = 16;
 std::mutex g_tune_mu;
-std::map<std::tuple<int, int, int, int>, int> g_tuned;
+std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_tuned;  // -> (split, pair)
 
 int num_sms() {
   static int n = 0;
@@ -829,22 +941,25 @@ void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, int split_req, long 
   const long nkb = std::max(1L, (k_estimate + BK - 1) / BK);
   const long ctas = (long)nt * (nt + 1) / 2 * 2 * nen;
   ws.tune_pending = 0;
+  ws.tune_split = ws.tune_pair = 0;
   ws.precision = precision;
-  if (split_req > 0) {
-    ws.nsplit = std::min(split_req, SPLIT_MAX);
-  } else if (ctas >= 2L * num_sms() || nkb < 2L * ksub_of(ws)) {
-    ws.nsplit = 1;
-  } else {
+  const bool split_fixed = split_req > 0 || ctas >= 2L * num_sms() || nkb < 2L * ksub_of(ws);
+  const bool pair_fixed = ws.pair_req != 0;
+  ws.nsplit = split_req > 0 ? std::min(split_req, SPLIT_MAX) : 1;
+  ws.pair = ws.pair_req == 2 ? 1 : 0;
+  if (!split_fixed || !pair_fixed) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     auto it = g_tuned.find(std::make_tuple(precision, Mp, nen, kbits(nkb)));
     if (it != g_tuned.end()) {
-      ws.nsplit = it->second;
+      if (!split_fixed) ws.nsplit = it->second.first;
+      if (!pair_fixed) ws.pair = it->second.second;
     } else {
-      ws.nsplit = 1;
       ws.tune_pending = 1;
+      ws.tune_split = split_fixed ? 0 : 1;
+      ws.tune_pair = pair_fixed ? 0 : 1;
     }
   }
-  ws.nslice = ws.tune_pending ? SPLIT_MAX : ws.nsplit;
+  ws.nslice = ws.tune_pending && ws.tune_split ? SPLIT_MAX : ws.nsplit;
   const size_t mbytes = sizeof(float2) * slice_of(Mp, nen) * ws.nslice;
   grow(ws.part, ws.part_bytes, mbytes);
   RP_CUDA(cudaMemsetAsync(ws.part, 0, mbytes, st));
@@ -870,7 +985,7 @@ thread_local GroupScratch g_scratch;
 struct GroupPlan {
   const TcArgs *probs = nullptr;
   const int4 *work = nullptr;
-  int nwork = 0, precision = 0;
+  int nwork = 0, precision = 0, pair = 0;
   size_t smem = 0;
 };
 
@@ -878,6 +993,9 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
   GroupPlan P;
   if (n <= 0) return P;
   P.precision = wss[0]->precision;
+  // CTA pairs when every problem of the group takes them
+  P.pair = 1;
+  for (int i = 0; i < n; i++) P.pair &= wss[i]->pair ? 1 : 0;
   std::vector<TcArgs> probs(n);
   // larger problems first, so the short ones fill the tail of the launch
   std::vector<int> order(n);
@@ -905,10 +1023,21 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
     a.kb_split = kb_split_of(nkb, std::min(ws.nsplit, ws.nslice), ksub);
     const int nsp = (nkb + a.kb_split - 1) / a.kb_split;
     if (nsp > ws.nslice) fail(1, "tensor-core group: %d K splits for %d slices", nsp, ws.nslice);
-    for (int ta = 0; ta < nt; ta++)
-      for (int tb = ta; tb < nt; tb++)
-        for (int sp = 0; sp < nsp; sp++)
-          for (int c = 0; c < 2 * ws.nen; c++) work.push_back(make_int4(i, ta | (tb << 16), c, sp));
+    if (P.pair) {
+      // row tiles 2 tp and 2 tp + 1 against column tiles tb >= 2 tp, the pair's
+      // two CTAs adjacent (nt is even: Mp = 2 Gp); (2 tp + 1, 2 tp) is below
+      // the diagonal and never read
+      for (int tp = 0; tp < nt / 2; tp++)
+        for (int tb = 2 * tp; tb < nt; tb++)
+          for (int sp = 0; sp < nsp; sp++)
+            for (int c = 0; c < 2 * ws.nen; c++)
+              for (int r = 0; r < 2; r++) work.push_back(make_int4(i, (2 * tp + r) | (tb << 16), c, sp));
+    } else {
+      for (int ta = 0; ta < nt; ta++)
+        for (int tb = ta; tb < nt; tb++)
+          for (int sp = 0; sp < nsp; sp++)
+            for (int c = 0; c < 2 * ws.nen; c++) work.push_back(make_int4(i, ta | (tb << 16), c, sp));
+    }
   }
   if (work.size() > 0x7fffffffu) fail(1, "tensor-core group: too many work items");
   const size_t pbytes = ((sizeof(TcArgs) * n + 255) / 256) * 256, wbytes = sizeof(int4) * work.size();
@@ -919,22 +1048,45 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
   P.probs = (const TcArgs *)dev;
   P.work = (const int4 *)((unsigned char *)dev + pbytes);
   P.nwork = (int)work.size();
-  P.smem = smem_of(P.precision);
+  P.smem = smem_of(P.precision, P.pair);
   if (P.smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", P.smem);
+  if (P.pair && P.nwork % 2) fail(1, "tensor-core group: odd work list for CTA pairs");
   return P;
 }
 
-void (*kernel_of(int precision))(TcGroup) {
-  if (precision == RP_PREC_FP16X3) return tc_gram_kernel<3, true, false>;
-  if (precision == RP_PREC_BF16X3) return tc_gram_kernel<3, true, true>;
-  return tc_gram_kernel<2, false, false>;
+void (*kernel_of(int precision, bool pair))(TcGroup) {
+  if (pair) {
+    if (precision == RP_PREC_FP16X3) return tc_gram_kernel<3, true, false, true>;
+    if (precision == RP_PREC_BF16X3) return tc_gram_kernel<3, true, true, true>;
+    return tc_gram_kernel<2, false, false, true>;
+  }
+  if (precision == RP_PREC_FP16X3) return tc_gram_kernel<3, true, false, false>;
+  if (precision == RP_PREC_BF16X3) return tc_gram_kernel<3, true, true, false>;
+  return tc_gram_kernel<2, false, false, false>;
 }
 
 int launch_group(const GroupPlan &P, int *err, cudaStream_t st) {
   if (P.nwork == 0) return 0;
-  void (*kern)(TcGroup) = kernel_of(P.precision);
+  void (*kern)(TcGroup) = kernel_of(P.precision, P.pair);
   TcGroup g{P.probs, P.work, err};
-  kern<<<(unsigned)P.nwork, NTHREADS, P.smem, st>>>(g);
+  if (P.pair) {
+    // clusters of two adjacent CTAs: work items 2i and 2i + 1
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)P.nwork);
+    cfg.blockDim = dim3(NTHREADS);
+    cfg.dynamicSmemBytes = P.smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    RP_CUDA(cudaLaunchKernelEx(&cfg, kern, g));
+  } else {
+    kern<<<(unsigned)P.nwork, NTHREADS, P.smem, st>>>(g);
+  }
   RP_CUDA(cudaGetLastError());
   return 1;
 }
@@ -943,37 +1095,48 @@ void set_kernel_smem(int precision) {
   static thread_local int done[4] = {0, 0, 0, 0};
   const int idx = precision & 3;
   if (done[idx]) return;
-  RP_CUDA(cudaFuncSetAttribute(kernel_of(precision), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               smem_cap(kernel_of(precision))));
+  for (int pair = 0; pair < 2; pair++)
+    RP_CUDA(cudaFuncSetAttribute(kernel_of(precision, pair), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem_cap(kernel_of(precision, pair))));
   done[idx] = 1;
 }
 
-// times every distinct split of the prepared batch, keeps the fastest
-void tune_split(TcWorkspace &ws, int *err, cudaStream_t st) {
+// times every candidate (split, pair) of the prepared batch, keeps the fastest
+void tune_shape(TcWorkspace &ws, int *err, cudaStream_t st) {
   const int nkb = ws.Kp / BK, ksub = ksub_of(ws);
-  std::vector<int> cands;
-  int last_nsp = 0;
-  for (int s = 1; s <= SPLIT_MAX; s *= 2) {
-    const int kbs = kb_split_of(nkb, s, ksub), nsp = (nkb + kbs - 1) / kbs;
-    if (nsp != last_nsp && nsp <= ws.nslice) cands.push_back(s);
-    last_nsp = nsp;
+  std::vector<int> splits;
+  if (ws.tune_split) {
+    int last_nsp = 0;
+    for (int s = 1; s <= SPLIT_MAX; s *= 2) {
+      const int kbs = kb_split_of(nkb, s, ksub), nsp = (nkb + kbs - 1) / kbs;
+      if (nsp != last_nsp && nsp <= ws.nslice) splits.push_back(s);
+      last_nsp = nsp;
+    }
+  } else {
+    splits.push_back(ws.nsplit);
   }
+  std::vector<int> pairs;
+  if (ws.tune_pair) pairs = {0, 1};
+  else pairs.push_back(ws.pair);
   TcWorkspace *one = &ws;
-  int best = 1;
+  int best_s = splits[0], best_p = pairs[0];
   float best_ms = 1e30f;
   for (int rep = 0; rep < 2; rep++)  // the first pass warms up
-    for (int s : cands) {
-      ws.nsplit = s;
-      GroupPlan P = plan_group(&one, 1, st, g_scratch.dev, g_scratch.bytes);
-      RP_CUDA(cudaEventRecord(ws.ev0, st));
-      launch_group(P, err, st);
-      RP_CUDA(cudaEventRecord(ws.ev1, st));
-      RP_CUDA(cudaEventSynchronize(ws.ev1));
-      float ms = 0;
-      RP_CUDA(cudaEventElapsedTime(&ms, ws.ev0, ws.ev1));
-      if (rep == 1 && ms < best_ms) { best_ms = ms; best = s; }
-    }
-  ws.nsplit = best;
+    for (int p : pairs)
+      for (int s : splits) {
+        ws.nsplit = s;
+        ws.pair = p;
+        GroupPlan P = plan_group(&one, 1, st, g_scratch.dev, g_scratch.bytes);
+        RP_CUDA(cudaEventRecord(ws.ev0, st));
+        launch_group(P, err, st);
+        RP_CUDA(cudaEventRecord(ws.ev1, st));
+        RP_CUDA(cudaEventSynchronize(ws.ev1));
+        float ms = 0;
+        RP_CUDA(cudaEventElapsedTime(&ms, ws.ev0, ws.ev1));
+        if (rep == 1 && ms < best_ms) { best_ms = ms; best_s = s; best_p = p; }
+      }
+  ws.nsplit = best_s;
+  ws.pair = best_p;
   ws.tune_pending = 0;
   // the candidates' sums are discarded
   RP_CUDA(cudaMemsetAsync(ws.part, 0, sizeof(float2) * slice_of(ws.Mp, ws.nen) * ws.nslice, st));
@@ -1037,9 +1200,9 @@ int tc_prepare(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const d
   if (ws.tune_pending) {
     const int kp_key = ws.Kp;  // the q's K estimate keys the cache
     ws.Kp = Kp;
-    tune_split(ws, err, st);
+    tune_shape(ws, err, st);
     std::lock_guard<std::mutex> g(g_tune_mu);
-    g_tuned[std::make_tuple(precision, Mp, nen, kbits(kp_key / BK))] = ws.nsplit;
+    g_tuned[std::make_tuple(precision, Mp, nen, kbits(kp_key / BK))] = std::make_pair(ws.nsplit, ws.pair);
   }
   ws.Kp = Kp;
   return launches;

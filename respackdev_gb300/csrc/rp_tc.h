@@ -19,7 +19,10 @@ struct TcWorkspace {
   int split_req = 0;        // K splits requested (0 = the tuner's choice)
   int nsplit = 1;           // K splits of the Gram launches of this q
   int nslice = 1;           // float-pair sum slices allocated (>= nsplit)
-  int tune_pending = 0;     // the first batch of this q times the split candidates
+  int tune_pending = 0;     // the first batch of this q times the launch-shape candidates
+  int tune_split = 0, tune_pair = 0;  // ... over the K split, over single CTAs / CTA pairs
+  int pair_req = 0;         // 0 the tuner's choice, 1 single CTAs, 2 CTA pairs (cta_group::2)
+  int pair = 0;             // the Gram launches of this q run CTA pairs
   // the prepared pair batch (tc_prepare)
   const float *Yt = nullptr, *sB = nullptr, *sA = nullptr;
   const float2 *wt = nullptr;
@@ -32,8 +35,9 @@ struct TcWorkspace {
 };
 
 // Allocates and zeroes the Gram sums of a q point.  split_req > 0 fixes the
-// number of K splits; 0 takes the tuner's cached choice for this shape or, for
-// a shape it has not seen, times the candidates on the first batch.
+// number of K splits and ws.pair_req != 0 the CTA shape; otherwise the tuner's
+// cached choice for this shape or, for a shape it has not seen, the fastest
+// candidate, timed on the first batch.
 void tc_begin_q(TcWorkspace &ws, int ng, int nen, int ndir, int split_req, long k_estimate, int precision,
                 cudaStream_t st);
 // Transposes and splits one pair batch into the workspace's operands and, at
@@ -61,7 +65,7 @@ int tc_end_q(TcWorkspace &ws, double2 *chi, double2 *rowcol, cudaStream_t st);
 double tc_group_run(TcWorkspace *const *ws, int n, double2 *const *chis, int *err, cudaStream_t st, bool graph,
                     long long *launches);
 
-// The split tuner's cache: number of shapes decided, and a reset (tests).
+// The launch-shape tuner's cache: number of shapes decided, and a reset (tests).
 int tc_tuned_shapes();
 void tc_reset_tuner();
 
