@@ -65,14 +65,19 @@ namespace {
 constexpr int BM = 128;          // tile rows (a) = TMEM lanes
 constexpr int BN = 128;          // tile columns (b)
 constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
-constexpr int NSTAGE = 2;
+constexpr int NSTAGE = 2;        // operand stages of a single CTA (a CTA pair, with half the B tile: 3)
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
 constexpr int NPROD = 512, NEPI = 128;    // 16 producer warps, 4 epilogue warps, MMA warp, loader warp
 constexpr int PROWS = BM / (NPROD / 32); // A rows per producer warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
-constexpr int WCHUNK = 16;                 // K blocks per weight chunk
-constexpr int WBYTES = WCHUNK * BK * 8;    // one channel's weights of a chunk (float2 per K)
+constexpr int WCHUNK = 16;                 // K blocks per weight chunk (a CTA pair: 4)
+// stages and weight chunk of a kernel variant
+__host__ __device__ constexpr int nstage_of(bool pair) { return pair ? 3 : NSTAGE; }
+// (the pair's three stages leave room for 4 K blocks of weights: the static
+// problem descriptor takes 1 KB of the opt-in total with the 1024-byte aligned
+// dynamic area)
+__host__ __device__ constexpr int wchunk_of(bool pair) { return pair ? WCHUNK / 4 : WCHUNK; }
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
 // One problem of a (possibly ragged) group: a prepared pair batch of one q.
@@ -379,17 +384,21 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int CG = PAIR ? 2 : 1;
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
+  constexpr int NST = nstage_of(PAIR), WCH = wchunk_of(PAIR), WB = WCH * BK * 8;
   constexpr int BTILE = PAIR ? TILE_BYTES / 2 : TILE_BYTES;  // this CTA's rows of a B plane tile
   constexpr int AOFF = 0, BOFF = NP * TILE_BYTES;
   constexpr int STAGE = NP * TILE_BYTES + NP * BTILE;  // A planes, B planes
   unsigned char *stage_base = smem;
-  unsigned char *wring = smem + (size_t)NSTAGE * STAGE;  // two weight chunks
-  uint64_t *bars = (uint64_t *)(wring + 2 * WBYTES);
-  uint64_t *full = bars, *bfull = bars + 2, *empty = bars + 4, *accfull = bars + 6, *accempty = bars + 8,
-           *wready = bars + 10, *wfree = bars + 12, *fin = bars + 14;
-  volatile int *abort_word = (volatile int *)(bars + 15);
-  uint32_t *tmem_slot = (uint32_t *)(bars + 16);
-  uint64_t *pready = bars + 18, *paccempty = bars + 20;  // the pair's relays (used in rank 0)
+  unsigned char *wring = smem + (size_t)NST * STAGE;  // two weight chunks
+  uint64_t *bars = (uint64_t *)(wring + 2 * WB);
+  // per stage: full (producers), bfull (loader), empty (MMAs done), pready (the
+  // pair's second CTA ready, used in rank 0); per accumulator buffer: accfull,
+  // accempty, paccempty (the second CTA's drain, rank 0); per weight chunk slot:
+  // wready, wfree
+  uint64_t *full = bars, *bfull = bars + 3, *empty = bars + 6, *pready = bars + 9, *accfull = bars + 12,
+           *accempty = bars + 14, *paccempty = bars + 16, *wready = bars + 18, *wfree = bars + 20, *fin = bars + 22;
+  volatile int *abort_word = (volatile int *)(bars + 23);
+  uint32_t *tmem_slot = (uint32_t *)(bars + 24);
   float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
   float *rB_s = sA_s + BM;                          // 1 / column scales of the B tile (128)
 
@@ -410,16 +419,18 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 
   if (tid == 0) {
     sh_args = grp.probs[wk.x];
-    for (int s = 0; s < NSTAGE; s++) {
+    for (int s = 0; s < NST; s++) {
       mbar_init(&full[s], NPROD);
       mbar_init(&bfull[s], 1);
       mbar_init(&empty[s], 1);
-      mbar_init(&accfull[s], 1);
-      mbar_init(&accempty[s], NEPI);
-      mbar_init(&wready[s], 1);
-      mbar_init(&wfree[s], NPROD);
       mbar_init(&pready[s], 1);
-      mbar_init(&paccempty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], NEPI);
+      mbar_init(&paccempty[b], 1);
+      mbar_init(&wready[b], 1);
+      mbar_init(&wfree[b], NPROD);
     }
     mbar_init(fin, 1);
     *abort_word = 0;
@@ -467,7 +478,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     for (int i = 0; i < PROWS; i++) cur[i] = __ldg(ya + i * rstride);
     const uint32_t cofs = (uint32_t)(lane & 3) * 4, chunk = (uint32_t)(lane >> 2);
     for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb & 1, use = kb >> 1;
+      const int s = kb % NST, use = kb / NST;
       if (kb + 1 < nkb) {
 #pragma unroll
         for (int i = 0; i < PROWS; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
@@ -477,12 +488,12 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 #pragma unroll
         for (int i = 0; i < PROWS; i++) prefetch_l2(ya + i * rstride + (size_t)(kb + PF_AHEAD) * (BK / 2));
       }
-      const int wc = kb / WCHUNK, kin = kb % WCHUNK;
+      const int wc = kb / WCH, kin = kb % WCH;
       if (kin == 0 && !mbar_wait(&wready[wc & 1], (wc >> 1) & 1, ab)) break;  // this chunk's weights
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, ab)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
       // (hi, lo) of K = 2 lane and 2 lane + 1
-      const float4 wv = *(const float4 *)(wring + (size_t)(wc & 1) * WBYTES + ((size_t)kin * BK + 2 * lane) * 8);
+      const float4 wv = *(const float4 *)(wring + (size_t)(wc & 1) * WB + ((size_t)kin * BK + 2 * lane) * 8);
       const float x0h = wv.x, x0l = wv.y, x1h = wv.z, x1l = wv.w;
 #pragma unroll
       for (int i = 0; i < PROWS; i++) {
@@ -500,7 +511,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       }
       fence_proxy_async();
       mbar_arrive(&full[s]);
-      if (kin == WCHUNK - 1 || kb == nkb - 1) mbar_arrive(&wfree[wc & 1]);  // done with this chunk's weights
+      if (kin == WCH - 1 || kb == nkb - 1) mbar_arrive(&wfree[wc & 1]);  // done with this chunk's weights
 #pragma unroll
       for (int i = 0; i < PROWS; i++) cur[i] = nxt[i];
     }
@@ -554,11 +565,11 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     if (PAIR && rank == 1) {
       // ---------------- the second CTA of a pair: relays to the issuer ----------------
       if (lane == 0) {
-        const uint32_t rp0 = cluster_addr(&pready[0], 0), rp1 = cluster_addr(&pready[1], 0);
+        const uint32_t rp0 = cluster_addr(&pready[0], 0);  // pready[s] is rp0 + 8 s
         for (int kb = 0; kb < nkb; kb++) {
-          const int s = kb & 1, use = kb >> 1;
+          const int s = kb % NST, use = kb / NST;
           if (!mbar_wait(&bfull[s], use & 1, ab) || !mbar_wait(&full[s], use & 1, ab)) break;
-          mbar_arrive_remote(s ? rp1 : rp0);
+          mbar_arrive_remote(rp0 + 8u * (uint32_t)s);
         }
       } else if (lane == 1) {
         const uint32_t ra0 = cluster_addr(&paccempty[0], 0), ra1 = cluster_addr(&paccempty[1], 0);
@@ -572,31 +583,30 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     } else if (lane == 0) {
       // ---------------- MMA issuer ----------------
       const uint32_t idesc = make_idesc(BF16 ? 1 : 0, PAIR ? 2 * BM : BM, BN);
-      // descriptors of every plane tile of both stages, built once: per MMA the
-      // issuing thread only adds the K step (32 bytes = 2 units of the start
-      // address), since it shares its sub-partition with busy producer warps
-      uint64_t dA0[NP], dA1[NP], dB0[NP], dB1[NP];
+      // descriptors of every plane tile of stage 0, built once: per MMA the
+      // issuing thread only adds the stage and the K step (32 bytes = 2 units of
+      // the start address, which stays below 2^14 units), since it shares its
+      // sub-partition with busy producer warps
+      uint64_t dA[NP], dB[NP];
       const uint32_t sb0 = smem_u32(stage_base);
 #pragma unroll
       for (int p = 0; p < NP; p++) {
-        dA0[p] = make_desc(sb0 + (uint32_t)(AOFF + p * TILE_BYTES));
-        dA1[p] = make_desc(sb0 + (uint32_t)(STAGE + AOFF + p * TILE_BYTES));
-        dB0[p] = make_desc(sb0 + (uint32_t)(BOFF + p * BTILE));
-        dB1[p] = make_desc(sb0 + (uint32_t)(STAGE + BOFF + p * BTILE));
+        dA[p] = make_desc(sb0 + (uint32_t)(AOFF + p * TILE_BYTES));
+        dB[p] = make_desc(sb0 + (uint32_t)(BOFF + p * BTILE));
       }
-      // the MMAs of one K block in stage S: products of planes pa (A) and pb (B)
+      // the MMAs of one K block in stage s: products of planes pa (A) and pb (B)
       // with pa + pb <= NP - 1, grouped by A plane (collector reuse); with the
       // exact scheme the leading product has its own accumulator.  The first
       // product into each accumulator of a sub-chunk overwrites it.
-      auto issue = [&](auto S_, bool fresh_block, uint32_t tacc) {
-        constexpr int S = decltype(S_)::value;
+      auto issue = [&](int s, bool fresh_block, uint32_t tacc) {
+        const uint64_t soff = (uint64_t)((uint32_t)s * (uint32_t)(STAGE >> 4));
 #pragma unroll
         for (int kk = 0; kk < BK / 16; kk++) {
           const bool fresh = fresh_block && kk == 0;
           auto prod = [&](auto PA_, auto PB_) {
             constexpr int pa = decltype(PA_)::value, pb = decltype(PB_)::value;
-            const uint64_t ad = (S == 0 ? dA0[pa] : dA1[pa]) + (uint64_t)(2 * kk);
-            const uint64_t bd = (S == 0 ? dB0[pb] : dB1[pb]) + (uint64_t)(2 * kk);
+            const uint64_t ad = dA[pa] + soff + (uint64_t)(2 * kk);
+            const uint64_t bd = dB[pb] + soff + (uint64_t)(2 * kk);
             constexpr bool main_acc = (EXACT && pa == 0 && pb == 0) || !EXACT;
             constexpr bool first = main_acc ? (pa == 0 && pb == 0) : (pa == 0 && pb == 1);
             mma_plane<pb, NP - pa, CG>(main_acc ? tacc : tacc + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
@@ -623,15 +633,14 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
         const int kbeg = sc * ksub, kend = min(nkb, kbeg + ksub);
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
-          const int s = kb & 1, use = kb >> 1;
+          const int s = kb % NST, use = kb / NST;
           if (!mbar_wait(&bfull[s], use & 1, ab) || !mbar_wait(&full[s], use & 1, ab) ||
               (PAIR && !mbar_wait<true>(&pready[s], use & 1, ab))) {
             ok = false;
             break;
           }
           tc_fence_after();
-          if (s == 0) issue(std::integral_constant<int, 0>{}, kb == kbeg, tacc);
-          else issue(std::integral_constant<int, 1>{}, kb == kbeg, tacc);
+          issue(s, kb == kbeg, tacc);
           mma_commit<CG>(&empty[s]);
         }
         if (!ok) break;
@@ -645,17 +654,17 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     // ---------------- loader: B planes per K block, weights per chunk, by bulk copy ----------------
     const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES + (size_t)rank * BTILE;
     const float2 *wsrc = a.wt + (size_t)cidx * a.Kp + (size_t)kb0 * BK;
-    const int nchunk = (nkb + WCHUNK - 1) / WCHUNK;
+    const int nchunk = (nkb + WCH - 1) / WCH;
     auto issue_w = [&](int c) {
-      const uint32_t bytes = (uint32_t)min(WCHUNK, nkb - c * WCHUNK) * BK * 8;
+      const uint32_t bytes = (uint32_t)min(WCH, nkb - c * WCH) * BK * 8;
       mbar_arrive_tx(&wready[c & 1], bytes);
-      bulk_g2s(wring + (size_t)(c & 1) * WBYTES, wsrc + (size_t)c * WCHUNK * BK, bytes, &wready[c & 1]);
+      bulk_g2s(wring + (size_t)(c & 1) * WB, wsrc + (size_t)c * WCH * BK, bytes, &wready[c & 1]);
     };
     issue_w(0);
     if (nchunk > 1) issue_w(1);
     int wnext = 2, issued = 0;
     for (int kb = 0; kb < nkb; kb++) {
-      const int s = kb & 1, use = kb >> 1;
+      const int s = kb % NST, use = kb / NST;
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, ab)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
       if (kb + PF_AHEAD < nkb) bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
@@ -665,7 +674,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
         bulk_g2s(st + BOFF + p * BTILE, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, BTILE, &bfull[s]);
       issued = kb + 1;
       // chunk wnext reuses the slot of chunk wnext - 2 once the producers have left it
-      if (wnext < nchunk && kb >= (wnext - 1) * WCHUNK) {
+      if (wnext < nchunk && kb >= (wnext - 1) * WCH) {
         if (!mbar_wait(&wfree[wnext & 1], ((wnext - 2) >> 1) & 1, ab)) break;
         issue_w(wnext);
         wnext++;
@@ -673,8 +682,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     }
     // after an abort, wait (bounded) for the copies still in flight before the CTA exits
     if (ab.up()) {
-      for (int kb = max(0, issued - NSTAGE); kb < issued; kb++)
-        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&bfull[kb & 1], (kb >> 1) & 1); i++) __nanosleep(32);
+      for (int kb = max(0, issued - NST); kb < issued; kb++)
+        for (long i = 0; i < WAIT_LIMIT && !mbar_try(&bfull[kb % NST], (kb / NST) & 1); i++) __nanosleep(32);
       for (int c = max(0, wnext - 2); c < wnext; c++)
         for (long i = 0; i < WAIT_LIMIT && !mbar_try(&wready[c & 1], (c >> 1) & 1); i++) __nanosleep(32);
     }
@@ -874,8 +883,8 @@ static size_t smem_of(int precision, bool pair) {
   // per stage: A planes, B planes (half a tile each in a CTA pair); the weight
   // ring; then the barriers and the scales
   const size_t np = (size_t)nplanes_of(precision);
-  return 1024 + (size_t)NSTAGE * np * (TILE_BYTES + (pair ? TILE_BYTES / 2 : TILE_BYTES)) + 2 * (size_t)WBYTES +
-         256 + 2 * sizeof(float) * BM;
+  return 1024 + (size_t)nstage_of(pair) * np * (TILE_BYTES + (pair ? TILE_BYTES / 2 : TILE_BYTES)) +
+         2 * (size_t)wchunk_of(pair) * BK * 8 + 256 + 2 * sizeof(float) * BM;
 }
 static size_t slice_of(int Mp, int nen) { return (size_t)nen * 2 * Mp * Mp; }
 // K blocks per FP32 sub-chunk: 1024 K by default; the integer leading plane's
@@ -989,6 +998,8 @@ struct GroupPlan {
   size_t smem = 0;
 };
 
+bool pairs_available(int precision);
+
 GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev, size_t &have) {
   GroupPlan P;
   if (n <= 0) return P;
@@ -1050,6 +1061,9 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
   P.nwork = (int)work.size();
   P.smem = smem_of(P.precision, P.pair);
   if (P.smem > 227 * 1024) fail(1, "tensor-core stage layout needs %zu bytes", P.smem);
+  if (P.pair && !pairs_available(P.precision))
+    fail(1, "tensor-core CTA pairs requested (tc_pair=2) but the device holds no cluster of two %zu-byte CTAs",
+         P.smem);
   if (P.pair && P.nwork % 2) fail(1, "tensor-core group: odd work list for CTA pairs");
   return P;
 }
@@ -1091,14 +1105,41 @@ int launch_group(const GroupPlan &P, int *err, cudaStream_t st) {
   return 1;
 }
 
+// clusters of the CTA-pair kernel of each precision the device can hold at once
+// (0: CTA pairs unavailable), set by set_kernel_smem
+thread_local int g_pair_clusters[4] = {-1, -1, -1, -1};
+
 void set_kernel_smem(int precision) {
-  static thread_local int done[4] = {0, 0, 0, 0};
   const int idx = precision & 3;
-  if (done[idx]) return;
-  for (int pair = 0; pair < 2; pair++)
+  if (g_pair_clusters[idx] >= 0) return;
+  for (int pair = 0; pair < 2; pair++) {
     RP_CUDA(cudaFuncSetAttribute(kernel_of(precision, pair), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  smem_cap(kernel_of(precision, pair))));
-  done[idx] = 1;
+    RP_CUDA(cudaFuncSetAttribute(kernel_of(precision, pair), cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * (unsigned)num_sms());
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = smem_of(precision, true);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel_of(precision, true), &cfg) != cudaSuccess) {
+    cudaGetLastError();  // not a sticky error: the pairs are just not offered
+    n = 0;
+  }
+  g_pair_clusters[idx] = n;
+}
+
+bool pairs_available(int precision) {
+  set_kernel_smem(precision);
+  return g_pair_clusters[precision & 3] > 0;
 }
 
 // times every candidate (split, pair) of the prepared batch, keeps the fastest
@@ -1116,8 +1157,8 @@ void tune_shape(TcWorkspace &ws, int *err, cudaStream_t st) {
     splits.push_back(ws.nsplit);
   }
   std::vector<int> pairs;
-  if (ws.tune_pair) pairs = {0, 1};
-  else pairs.push_back(ws.pair);
+  if (ws.tune_pair && pairs_available(ws.precision)) pairs = {0, 1};
+  else pairs.push_back(ws.tune_pair ? 0 : ws.pair);
   TcWorkspace *one = &ws;
   int best_s = splits[0], best_p = pairs[0];
   float best_ms = 1e30f;
