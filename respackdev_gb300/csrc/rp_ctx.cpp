@@ -79,7 +79,7 @@ struct rp_ctx {
   DevBuf slot_of, win_bands;
   // per-q device data
   DevBuf kpq, shift, lg0, qglen, pvir, pocc, chunk_vir, chunk_first, chunk_count, pair_list, wts, rho, head, chi,
-      rowcol, A, eps, prow, fcol, piv, used, intra, pwpl, mixws, mixaux;
+      rowcol, A, eps, prow, piv, used, intra, pwpl, mixws, mixaux;
   rp::TcWorkspace tcw;
   // band-tail network (&param_gpu tail_model): the network, its shell count and
   // target scale, the excluded-band statistics, and the per-q shell map,
@@ -104,7 +104,7 @@ struct rp_ctx {
   ~rp_ctx() {
     for (DevBuf *b : {&coef, &numirr, &trs, &src, &phase, &ng0, &kg0, &cfull, &ur, &energy, &prob, &imt1, &index2, &em,
                       &b9, &sk0, &errw, &inc_off, &inc, &kpq, &shift, &lg0, &qglen, &pvir, &pocc, &chunk_vir, &chunk_first,
-                      &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &fcol, &piv, &used,
+                      &chunk_count, &pair_list, &wts, &rho, &head, &chi, &rowcol, &A, &eps, &prow, &piv, &used,
                       &intra, &pwpl, &mixws, &mixaux, &tail_sh, &tail_x, &slot_of, &win_bands})
       b->release();
     tcw.release();
@@ -653,8 +653,7 @@ static void epsinv_run(rp_ctx *c) {
   cudaStream_t st = c->st;
   c->A.ensure(sizeof(cd) * sz);
   c->eps.ensure(sizeof(cd) * sz);
-  c->prow.ensure(sizeof(cd) * (size_t)nmat * ng);
-  c->fcol.ensure(sizeof(cd) * ((size_t)nmat * ng + nmat));  // pivot column copies + pivot reciprocals
+  c->prow.ensure(rp::gauss_jordan_scratch_bytes(ng, nmat));  // the Gauss-Jordan panels' pivot rows
   c->piv.ensure(sizeof(int) * (size_t)nmat * ng);
   c->used.ensure(sizeof(int) * (size_t)nmat * ng);
   rp::EpsArgs a;
@@ -687,9 +686,8 @@ static void epsinv_run(rp_ctx *c) {
     fp64 = !ok;
   }
   if (fp64)
-    c->launches += rp::launch_gauss_jordan(c->A.as<double2>(), ng, nmat, c->prow.as<double2>(), c->fcol.as<double2>(),
-                                           c->piv.as<int>(), c->used.as<int>(), c->eps.as<double2>(),
-                                           c->errw.as<int>(), st);
+    c->launches += rp::launch_gauss_jordan(c->A.as<double2>(), ng, nmat, c->prow.as<double2>(), c->piv.as<int>(),
+                                           c->used.as<int>(), c->eps.as<double2>(), c->errw.as<int>(), st);
   RP_CUDA(cudaEventRecord(c->ev[1], st));
   check_device_error(c);
   float ms = 0;

@@ -171,8 +171,12 @@ struct EpsArgs {
   double wd[3], delt;
 };
 int launch_eps_build(const double2 *chi, const EpsArgs &a, double2 *A, cudaStream_t st);
-int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prow, double2 *fcol, int *piv, int *used,
-                        double2 *out, int *err, cudaStream_t st);
+// FP64 blocked Gauss-Jordan of the nmat matrices A (n x n, column-major, in
+// place; the unscrambled inverse into out); prows holds
+// gauss_jordan_scratch_bytes, piv and used n ints per matrix.
+size_t gauss_jordan_scratch_bytes(int n, int nmat);
+int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prows, int *piv, int *used, double2 *out, int *err,
+                        cudaStream_t st);
 // Mixed-precision inverse of the nmat matrices A (n x n, column-major): FP32
 // Gauss-Jordan, a float-pair residual R = I - A X0 and one Newton step.
 // rnorm[m] receives |R|_F^2 of matrix m (device); ws holds epsinv_mixed_bytes.

@@ -7,10 +7,10 @@
 // w = Re(em), 1e-5 when zero), wings divided by one |q+G| only.
 // invZGE (invZGE.F90:1-22) inverts with LAPACK zgetrf + zgetri; here every
 // (frequency, direction) matrix is inverted by Gauss-Jordan elimination with
-// partial pivoting on |re|+|im| (izamax's norm), one kernel pair per pivot
-// column over all matrices at once, and the row/column permutation undone at
-// the end.  The select kernel scales the pivot column by the pivot's
-// reciprocal once, so the update is four FP64 FMAs per element.
+// partial pivoting on |re|+|im| (izamax's norm), all matrices at once, and the
+// row/column permutation undone at the end.  The pivot steps run in panels of
+// b columns: a panel's steps in shared memory (one CTA per matrix), then one
+// rank-b update of every other column (blocked_gauss_jordan below).
 #include "rp_dev.cuh"
 #include "rp_host.h"
 
@@ -72,85 +72,182 @@ __device__ __forceinline__ typename C2<T>::t crecip(typename C2<T>::t b) {
   return mk<T>(t / d, (T)-1 / d);
 }
 
-// T = double: the inverse itself; T = float: the first approximation of the
-// mixed-precision inverse below
+// ---------------------------------------------------------------------------
+// Blocked Gauss-Jordan.  The b pivot steps k0 .. k0 + b - 1 touch every column,
+// but only the panel's own columns decide the pivots.  So the panel runs its b
+// steps alone (gj_panel_kernel), and the other columns T take the b steps at
+// once: with P the panel's pivot rows, GJ leaves in panel column t the image
+// of the unit vector e_{P_t} under the b steps, and every column x transforms
+// as x <- x - (E_P - Pan) x_P, i.e.
+//   A[:,T] <- (A[:,T] with rows P zeroed) + Pan A_old[P,T]
+// (gj_trail_kernel, A_old[P,T] copied by the panel kernel before the update).
+// Per element the same operations as the one-step-at-a-time elimination up to
+// the order of the b-term sums; the matrices are read and written once per
+// panel instead of once per pivot.
+
+// widest panel: 32 columns in FP32, 16 in FP64 (the trailing update's 64-row
+// tiles of the panel and the pivot rows stay within 32 KB of shared memory)
 template <typename T>
-__global__ void gj_select_kernel(typename C2<T>::t *__restrict__ A, int n, int k, typename C2<T>::t *__restrict__ prow,
-                                 typename C2<T>::t *__restrict__ fcol, int *__restrict__ piv, int *__restrict__ used,
-                                 typename C2<T>::t *__restrict__ dinv, int *__restrict__ err) {
+constexpr int panel_max() { return sizeof(T) == 4 ? 32 : 16; }
+
+// panel width for n: the panel (b columns), the scaled pivot column and the
+// row flags in shared memory
+template <typename T>
+int panel_width(int n) {
+  const long avail = 200L * 1024 - (long)n * (sizeof(typename C2<T>::t) + sizeof(int));
+  long b = avail / ((long)n * (long)sizeof(typename C2<T>::t));
+  b = b > panel_max<T>() ? panel_max<T>() : b;
+  return b < 1 ? 1 : (int)b;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) gj_panel_kernel(typename C2<T>::t *__restrict__ A, int n, int k0, int b,
+                                                       int *__restrict__ piv, int *__restrict__ used,
+                                                       typename C2<T>::t *__restrict__ prows, int *__restrict__ err) {
   using T2 = typename C2<T>::t;
-  const int m = blockIdx.x;
+  const int m = blockIdx.x, tid = threadIdx.x, nth = blockDim.x;
   const size_t nn = (size_t)n * n;
   T2 *Am = A + m * nn;
   int *um = used + (size_t)m * n;
-  __shared__ T sv[256];
-  __shared__ int si[256];
-  T best = -1;
-  int bi = 0x7fffffff;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    if (um[i]) continue;
-    T2 v = Am[i + (size_t)n * k];
-    T s = fabs(v.x) + fabs(v.y);
-    if (s > best || (s == best && i < bi)) { best = s; bi = i; }
+  int *pm = piv + (size_t)m * n;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T2 *pan = (T2 *)smem;                 // [t][i]: panel column t
+  T2 *fc = pan + (size_t)b * n;         // the pivot column times the pivot's reciprocal
+  int *us = (int *)(fc + n);            // rows used as pivots
+  __shared__ T sv[32];
+  __shared__ int si[32];
+  __shared__ T2 prow[panel_max<T>()], sd;
+  __shared__ int sp;
+  for (size_t l = tid; l < (size_t)b * n; l += nth) {
+    const int i = (int)(l % n), t = (int)(l / n);
+    pan[l] = Am[i + (size_t)n * (k0 + t)];
   }
-  sv[threadIdx.x] = best;
-  si[threadIdx.x] = bi;
+  for (int i = tid; i < n; i += nth) us[i] = um[i];
   __syncthreads();
-  for (int s = blockDim.x / 2; s; s >>= 1) {
-    if (threadIdx.x < s) {
-      T ob = sv[threadIdx.x + s];
-      int oi = si[threadIdx.x + s];
-      if (ob > sv[threadIdx.x] || (ob == sv[threadIdx.x] && oi < si[threadIdx.x])) { sv[threadIdx.x] = ob; si[threadIdx.x] = oi; }
+  for (int t = 0; t < b; t++) {
+    // pivot: the largest |re|+|im| of column t among unused rows, lowest row on ties
+    T best = -1;
+    int bi = 0x7fffffff;
+    for (int i = tid; i < n; i += nth) {
+      if (us[i]) continue;
+      const T2 v = pan[(size_t)t * n + i];
+      const T s = fabs(v.x) + fabs(v.y);
+      if (s > best || (s == best && i < bi)) { best = s; bi = i; }
+    }
+    for (int o = 16; o; o >>= 1) {
+      const T ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if ((tid & 31) == 0) { sv[tid >> 5] = best; si[tid >> 5] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      for (int w = 1; w < (nth >> 5); w++)
+        if (sv[w] > best || (sv[w] == best && si[w] < bi)) { best = sv[w]; bi = si[w]; }
+      // NaN entries never win the comparison: fall back to row k's slot and flag
+      const int k = k0 + t;
+      const int p = (bi >= 0 && bi < n) ? bi : k;
+      if (!(best > (T)0) || bi != p) atomicExch(err, 3);
+      pm[k] = p;
+      us[p] = 1;
+      const T2 pk = pan[(size_t)t * n + p];
+      sd = (pk.x == (T)0 && pk.y == (T)0) ? mk<T>(0, 0) : crecip<T>(pk);
+      sp = p;
+    }
+    __syncthreads();
+    const T2 d = sd;
+    const int p = sp;
+    if (d.x == (T)0 && d.y == (T)0) continue;  // singular: flagged above
+    if (tid < b) prow[tid] = pan[(size_t)tid * n + p];
+    for (int i = tid; i < n; i += nth) fc[i] = cmul(pan[(size_t)t * n + i], d);
+    __syncthreads();
+    for (size_t l = tid; l < (size_t)b * n; l += nth) {
+      const int i = (int)(l % n), j = (int)(l / n);
+      T2 &a = pan[l];
+      const T2 pj = prow[j];
+      if (i == p) {
+        a = (j == t) ? d : cmul(pj, d);
+      } else if (j == t) {
+        a = mk<T>(-fc[i].x, -fc[i].y);
+      } else {
+        const T2 f = fc[i];
+        a.x = fma(-f.x, pj.x, a.x); a.x = fma(f.y, pj.y, a.x);
+        a.y = fma(-f.x, pj.y, a.y); a.y = fma(-f.y, pj.x, a.y);
+      }
     }
     __syncthreads();
   }
-  // NaN entries never win the comparison: fall back to row k's slot and flag
-  const int p = (si[0] >= 0 && si[0] < n) ? si[0] : k;
-  __shared__ T2 sd;
-  if (threadIdx.x == 0) {
-    if (!(sv[0] > (T)0) || si[0] != p) atomicExch(err, 3);
-    piv[(size_t)m * n + k] = p;
-    um[p] = 1;
-    const T2 pk = Am[p + (size_t)n * k];
-    sd = (pk.x == (T)0 && pk.y == (T)0) ? mk<T>(0, 0) : crecip<T>(pk);
-    dinv[m] = sd;
+  for (size_t l = tid; l < (size_t)b * n; l += nth) {
+    const int i = (int)(l % n), t = (int)(l / n);
+    Am[i + (size_t)n * (k0 + t)] = pan[l];
   }
-  __syncthreads();
-  const T2 d = sd;
-  // prow: the pivot row; fcol: the pivot column times the pivot's reciprocal
-  for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    prow[(size_t)m * n + j] = Am[p + (size_t)n * j];
-    fcol[(size_t)m * n + j] = cmul(Am[j + (size_t)n * k], d);
+  for (int i = tid; i < n; i += nth) um[i] = us[i];
+  // the pivot rows outside the panel, before the trailing update: prows[m][t][j]
+  T2 *pr = prows + (size_t)m * b * n;
+  for (size_t l = tid; l < (size_t)b * n; l += nth) {
+    const int j = (int)(l % n), t = (int)(l / n);
+    if (j >= k0 && j < k0 + b) continue;
+    pr[l] = Am[pm[k0 + t] + (size_t)n * j];
   }
 }
 
-// one pivot step on all matrices: block (32 rows x 8 columns) of matrix blockIdx.z
+constexpr int TT = 64;  // trailing-update tile (TT x TT per CTA, 4 x 4 per thread)
+
+// A[:,T] <- (A[:,T] with the panel's pivot rows zeroed) + Pan A_old[P,T]
 template <typename T>
-__global__ void __launch_bounds__(256) gj_update_kernel(typename C2<T>::t *__restrict__ A, int n, int k,
-                                                        const typename C2<T>::t *__restrict__ prow,
-                                                        const typename C2<T>::t *__restrict__ fcol,
-                                                        const int *__restrict__ piv,
-                                                        const typename C2<T>::t *__restrict__ dinv) {
+__global__ void __launch_bounds__(256) gj_trail_kernel(typename C2<T>::t *__restrict__ A, int n, int k0, int b,
+                                                       const int *__restrict__ piv,
+                                                       const typename C2<T>::t *__restrict__ prows) {
   using T2 = typename C2<T>::t;
-  const int m = blockIdx.z;
-  const int i = blockIdx.x * 32 + threadIdx.x, j = blockIdx.y * 8 + threadIdx.y;
-  if (i >= n || j >= n) return;
-  const int p = piv[(size_t)m * n + k];
-  const T2 d = dinv[m];
-  if (d.x == (T)0 && d.y == (T)0) return;  // singular: flagged by the select kernel
-  T2 *a = A + (size_t)m * n * n + i + (size_t)n * j;
-  const T2 pj = prow[(size_t)m * n + j];
-  if (i == p) {
-    *a = (j == k) ? d : cmul(pj, d);
-  } else {
-    const T2 f = fcol[(size_t)m * n + i];
-    if (j == k) {
-      *a = mk<T>(-f.x, -f.y);
-    } else {
-      T2 v = *a;  // a - f pj in four FMAs
-      v.x = fma(-f.x, pj.x, v.x); v.x = fma(f.y, pj.y, v.x);
-      v.y = fma(-f.x, pj.y, v.y); v.y = fma(-f.y, pj.x, v.y);
-      *a = v;
+  const int m = blockIdx.z, i0 = blockIdx.x * TT, j0 = blockIdx.y * TT, tid = threadIdx.x;
+  // a tile of panel columns only: nothing to do
+  if (j0 >= k0 && j0 + TT <= k0 + b) return;
+  const size_t nn = (size_t)n * n;
+  T2 *Am = A + m * nn;
+  const T2 *pr = prows + (size_t)m * b * n;
+  __shared__ T2 Ps[panel_max<T>()][TT];   // panel rows i0 .., column t
+  __shared__ T2 Rs[panel_max<T>()][TT];   // pivot row t, columns j0 ..
+  __shared__ int isp[TT];
+  if (tid < TT) isp[tid] = 0;
+  __syncthreads();
+  if (tid < b) {
+    const int p = piv[(size_t)m * n + k0 + tid];
+    if (p >= i0 && p < i0 + TT) isp[p - i0] = 1;
+  }
+  for (int l = tid; l < b * TT; l += 256) {
+    const int r = l % TT, t = l / TT;
+    Ps[t][r] = (i0 + r < n) ? Am[(i0 + r) + (size_t)n * (k0 + t)] : mk<T>(0, 0);
+    Rs[t][r] = (j0 + r < n) ? pr[(size_t)t * n + j0 + r] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  const int ti = tid & 15, tj = tid >> 4;
+  T2 acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int c = 0; c < 4; c++) acc[a][c] = mk<T>(0, 0);
+  for (int t = 0; t < b; t++) {
+    T2 pv[4], rv[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) pv[a] = Ps[t][ti + 16 * a];
+#pragma unroll
+    for (int c = 0; c < 4; c++) rv[c] = Rs[t][tj + 16 * c];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int c = 0; c < 4; c++) cfma(acc[a][c], pv[a], rv[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    const int j = j0 + tj + 16 * c;
+    if (j >= n || (j >= k0 && j < k0 + b)) continue;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      const int r = ti + 16 * a, i = i0 + r;
+      if (i >= n) continue;
+      T2 *x = Am + i + (size_t)n * j;
+      const T2 v = isp[r] ? mk<T>(0, 0) : *x;
+      *x = mk<T>(v.x + acc[a][c].x, v.y + acc[a][c].y);
     }
   }
 }
@@ -183,31 +280,42 @@ int launch_eps_build(const double2 *chi, const EpsArgs &a, double2 *A, cudaStrea
   return 1;
 }
 
+// Blocked Gauss-Jordan of nmat matrices (n x n, column-major, consecutive) in
+// place, then the unscrambled inverse into out.  prows: nmat * panel_width(n) * n scratch.
 template <typename T>
-static int gauss_jordan(typename C2<T>::t *A, int n, int nmat, typename C2<T>::t *prow, typename C2<T>::t *fcol,
-                        int *piv, int *used, typename C2<T>::t *out, int *err, cudaStream_t st) {
+static int blocked_gauss_jordan(typename C2<T>::t *A, int n, int nmat, typename C2<T>::t *prows, int *piv, int *used,
+                                typename C2<T>::t *out, int *err, cudaStream_t st) {
+  using T2 = typename C2<T>::t;
   int launches = 0;
   RP_CUDA(cudaMemsetAsync(used, 0, sizeof(int) * (size_t)n * nmat, st));
-  const size_t nn = (size_t)n * n;
-  // reciprocals of the pivots live after the pivot column copies
-  typename C2<T>::t *dinv = fcol + (size_t)nmat * n;
-  dim3 ublk(32, 8), ugrid2((n + 31) / 32, (n + 7) / 8, nmat);
-  dim3 ugrid((unsigned)std::min<size_t>((nn + 255) / 256, 2048), nmat);
-  for (int k = 0; k < n; k++) {
-    gj_select_kernel<T><<<nmat, 256, 0, st>>>(A, n, k, prow, fcol, piv, used, dinv, err);
-    gj_update_kernel<T><<<ugrid2, ublk, 0, st>>>(A, n, k, prow, fcol, piv, dinv);
+  const int bw = panel_width<T>(n);
+  const size_t psmem = ((size_t)bw + 1) * n * sizeof(T2) + sizeof(int) * (size_t)n;
+  if (psmem > 227 * 1024) fail(1, "Gauss-Jordan panel of n = %d does not fit in shared memory", n);
+  RP_CUDA(cudaFuncSetAttribute(gj_panel_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               smem_cap(gj_panel_kernel<T>)));
+  dim3 tgrid((n + TT - 1) / TT, (n + TT - 1) / TT, nmat);
+  for (int k0 = 0; k0 < n; k0 += bw) {
+    const int b = std::min(bw, n - k0);
+    gj_panel_kernel<T><<<nmat, 512, psmem, st>>>(A, n, k0, b, piv, used, prows, err);
+    gj_trail_kernel<T><<<tgrid, 256, 0, st>>>(A, n, k0, b, piv, prows);
     launches += 2;
   }
   RP_CUDA(cudaGetLastError());
   // `used` doubles as the inverse-permutation scratch of the unscramble step
+  const size_t nn = (size_t)n * n;
+  dim3 ugrid((unsigned)std::min<size_t>((nn + 255) / 256, 2048), nmat);
   gj_unscramble_kernel<<<ugrid, 256, sizeof(int) * n, st>>>(A, n, piv, used, out);
   RP_CUDA(cudaGetLastError());
   return launches + 1;
 }
 
-int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prow, double2 *fcol, int *piv, int *used,
-                        double2 *out, int *err, cudaStream_t st) {
-  return gauss_jordan<double>(A, n, nmat, prow, fcol, piv, used, out, err, st);
+size_t gauss_jordan_scratch_bytes(int n, int nmat) {
+  return sizeof(double2) * (size_t)nmat * panel_width<double>(n) * n;
+}
+
+int launch_gauss_jordan(double2 *A, int n, int nmat, double2 *prows, int *piv, int *used, double2 *out, int *err,
+                        cudaStream_t st) {
+  return blocked_gauss_jordan<double>(A, n, nmat, prows, piv, used, out, err, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -360,7 +468,7 @@ __global__ void __launch_bounds__(256) correct_kernel(const float2 *__restrict__
 
 size_t epsinv_mixed_bytes(int n, int nmat) {
   const size_t nn = (size_t)n * n * nmat;
-  return sizeof(float4) * nn + sizeof(float2) * (3 * nn + 2 * (size_t)n * nmat + nmat);
+  return sizeof(float4) * nn + sizeof(float2) * (3 * nn + (size_t)nmat * panel_width<float>(n) * n);
 }
 
 int launch_epsinv_mixed(const double2 *A, int n, int nmat, void *ws, int *piv, int *used, double2 *out,
@@ -368,11 +476,11 @@ int launch_epsinv_mixed(const double2 *A, int n, int nmat, void *ws, int *piv, i
   const size_t nn = (size_t)n * n * nmat;
   float4 *Ahl = (float4 *)ws;
   float2 *A32 = (float2 *)(Ahl + nn), *X0 = A32 + nn, *R = X0 + nn;
-  float2 *prow = R + nn, *fcol = prow + (size_t)n * nmat;  // fcol holds nmat reciprocals after the columns
+  float2 *prows = R + nn;  // the panels' pivot rows
   int launches = 0;
   split_f32_kernel<<<2048, 256, 0, st>>>(A, nn, A32, Ahl);
   launches++;
-  launches += gauss_jordan<float>(A32, n, nmat, prow, fcol, piv, used, X0, err, st);
+  launches += blocked_gauss_jordan<float>(A32, n, nmat, prows, piv, used, X0, err, st);
   RP_CUDA(cudaMemsetAsync(rnorm, 0, sizeof(float) * nmat, st));
   dim3 g((n + MT - 1) / MT, (n + MT - 1) / MT, nmat);
   resid_ff_kernel<<<g, 256, 0, st>>>(Ahl, X0, n, R, rnorm);
