@@ -16,12 +16,13 @@
 // 16-bit floating terms of the same row units, keeping the six products with
 // plane(A) + plane(B) <= 2.  The tensor core's FP32 accumulator does not round
 // to nearest, so the products of integer leading terms go to their own
-// accumulator: their partial sums are integers below 2^24 over a sub-chunk of
-// up to 1024 K and stay exact; the five correction products, about 2^-7
-// smaller, go to a second accumulator.  The accumulators are double-buffered
-// in tensor memory: while the tensor core fills one pair for sub-chunk s + 1,
-// the epilogue warps take sub-chunk s out of the other, unscale it (powers of
-// two: exact) and add it with TwoSum into a float-pair copy of the tile in
+// accumulator: their partial sums are integers of at most 2^24 over a
+// sub-chunk of up to 1024 K; the five correction products, about 2^-7
+// smaller, go to a second accumulator.  On single CTAs the
+// accumulators are double-buffered in tensor memory: while the tensor core
+// fills one pair for sub-chunk s + 1, the epilogue warps take sub-chunk s out
+// of the other, unscale it (powers of two: exact) and add it with TwoSum into
+// a float-pair copy of the tile in
 // global memory (tile-blocked, rows contiguous, so a warp's 32 rows are one
 // coalesced access), converted to FP64 once when chi is assembled.
 //
@@ -65,19 +66,21 @@ namespace {
 constexpr int BM = 128;          // tile rows (a) = TMEM lanes
 constexpr int BN = 128;          // tile columns (b)
 constexpr int BK = 64;           // K per stage (one 128-byte swizzle row of 16-bit values)
-constexpr int NSTAGE = 2;        // operand stages of a single CTA (a CTA pair, with half the B tile: 3)
+constexpr int NSTAGE = 2;        // operand stages
 constexpr int TILE_BYTES = BM * BK * 2;  // 16 KB per operand plane tile
 constexpr int NPROD = 512, NEPI = 128;    // 16 producer warps, 4 epilogue warps, MMA warp, loader warp
 constexpr int PROWS = BM / (NPROD / 32); // A rows per producer warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
-constexpr int WCHUNK = 16;                 // K blocks per weight chunk (a CTA pair: 4)
+constexpr int WCHUNK = 16;                 // K blocks per weight chunk
 // stages and weight chunk of a kernel variant
-__host__ __device__ constexpr int nstage_of(bool pair) { return pair ? 3 : NSTAGE; }
-// (the pair's three stages leave room for 4 K blocks of weights: the static
-// problem descriptor takes 1 KB of the opt-in total with the 1024-byte aligned
-// dynamic area)
-__host__ __device__ constexpr int wchunk_of(bool pair) { return pair ? WCHUNK / 4 : WCHUNK; }
+__host__ __device__ constexpr int nstage_of(bool) { return NSTAGE; }
+__host__ __device__ constexpr int wchunk_of(bool) { return WCHUNK; }
+// accumulator columns of a CTA (a CTA pair: both column tiles of its 2 x 2
+// block) and tensor-memory buffers of them (a pair: one, its two accumulators
+// of 256 columns fill the 512)
+__host__ __device__ constexpr int nb_of(bool pair) { return pair ? 2 * BN : BN; }
+__host__ __device__ constexpr int nbuf_of(bool pair) { return pair ? 1 : 2; }
 constexpr long WAIT_LIMIT = 1L << 28;    // polls before a wait gives up
 
 // One problem of a (possibly ragged) group: a prepared pair batch of one q.
@@ -366,16 +369,18 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // work item (problem, upper tile, frequency, Re/Im weight, K split); see the
 // file comment for the roles.
 //
-// PAIR: a cluster of two CTAs computes the 256 x 128 block of rows ta, ta + 1
-// (work items 2i, 2i + 1) and columns tb with tcgen05.mma.cta_group::2.  Each
-// CTA produces its own 128 A rows and bulk-copies half of the B tile (64 of
-// its 128 rows: the first or second 8 KB of each 128-byte-swizzled plane
-// tile), so a pair reads and writes a third less shared memory per product
-// than two single CTAs, and one thread issues the MMAs of both.  The first CTA
-// (rank 0) issues; its commits arrive on the barriers of both CTAs.  The
-// second CTA's MMA warp relays to the first: lane 0 that a stage of its
-// operands is ready (pready), lane 1 that its epilogue has drained an
-// accumulator buffer (paccempty).
+// PAIR: a cluster of two CTAs computes a 2 x 2 block of tiles, rows 2 tpa,
+// 2 tpa + 1 and columns 2 tpb, 2 tpb + 1 (work items 2i, 2i + 1), with
+// tcgen05.mma.cta_group::2 of 256 x 256: CTA r produces row tile 2 tpa + r of
+// the weighted operand and bulk-copies column tile 2 tpb + r of B, and each
+// CTA's tensor memory takes its row tile against both column tiles.  So a
+// produced A plane and a loaded B plane each serve twice the products of a
+// single CTA, and one thread issues the MMAs of both CTAs.  The two
+// accumulators of 256 columns fill tensor memory, so the MMAs of a sub-chunk
+// wait for the drain of the previous one.  The first CTA (rank 0)
+// issues; its commits arrive on the barriers of both CTAs.  The second CTA's
+// MMA warp relays to the first: lane 0 that a stage of its operands is ready
+// (pready), lane 1 that its epilogue has drained the accumulators (paccempty).
 template <int NP, bool EXACT, bool BF16, bool PAIR>
 // 22 warps: at most 6 on one SM sub-partition, whose 16K registers allow 85 per thread
 __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
@@ -385,9 +390,9 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   constexpr int CG = PAIR ? 2 : 1;
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
   constexpr int NST = nstage_of(PAIR), WCH = wchunk_of(PAIR), WB = WCH * BK * 8;
-  constexpr int BTILE = PAIR ? TILE_BYTES / 2 : TILE_BYTES;  // this CTA's rows of a B plane tile
+  constexpr int NB = nb_of(PAIR), NBUF = nbuf_of(PAIR);  // accumulator columns, buffers
   constexpr int AOFF = 0, BOFF = NP * TILE_BYTES;
-  constexpr int STAGE = NP * TILE_BYTES + NP * BTILE;  // A planes, B planes
+  constexpr int STAGE = 2 * NP * TILE_BYTES;        // A planes, B planes
   unsigned char *stage_base = smem;
   unsigned char *wring = smem + (size_t)NST * STAGE;  // two weight chunks
   uint64_t *bars = (uint64_t *)(wring + 2 * WB);
@@ -400,7 +405,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   volatile int *abort_word = (volatile int *)(bars + 23);
   uint32_t *tmem_slot = (uint32_t *)(bars + 24);
   float *sA_s = (float *)(bars + 32);               // row scales of this CTA's A rows (128)
-  float *rB_s = sA_s + BM;                          // 1 / column scales of the B tile (128)
+  float *rB_s = sA_s + BM;                          // 1 / column scales of the accumulator columns (NB)
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t rank = PAIR ? cluster_rank() : 0;
@@ -408,7 +413,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   // the work list has channels fastest, so the CTAs running together share their operand rows in L2
   const int4 wk = grp.work[blockIdx.x];
   const TcArgs &a = sh_args;
-  const int ta = wk.y & 0xffff, tb = wk.y >> 16;
+  const int ta = wk.y & 0xffff, tb = wk.y >> 16;     // this CTA's row tile and B tile
+  const int tb0 = PAIR ? (tb & ~1) : tb;               // the first column tile of the accumulators
   const int cidx = wk.z, e = cidx >> 1, ch = cidx & 1;  // frequency, channel (0 = Re weight, 1 = Im weight)
   {
     // empty K range (the host makes none): the whole CTA leaves, and so does
@@ -458,10 +464,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   const int nkb = min(nkb_all - kb0, a.kb_split);
   const int ksub = a.ksub_blocks;
   const int nsub = (nkb + ksub - 1) / ksub;
-  for (int i = tid; i < BM; i += NTHREADS) {
-    sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
-    rB_s[i] = 1.0f / a.sB[tb * BN + i];  // exact: a power of two
-  }
+  for (int i = tid; i < BM; i += NTHREADS) sA_s[i] = a.sA[(size_t)cidx * a.Mp + ta * BM + i];
+  for (int i = tid; i < NB; i += NTHREADS) rB_s[i] = 1.0f / a.sB[tb0 * BN + i];  // exact: a power of two
   __syncthreads();
 
   if (warp < NPROD / 32) {
@@ -516,8 +520,8 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       for (int i = 0; i < PROWS; i++) cur[i] = nxt[i];
     }
   } else if (warp < MMA_WARP) {
-    // ---------------- epilogue: each sub-chunk into the float-pair tile ----------------
-    // TMEM columns: buffer b holds [main][corr (exact scheme)] at b * NACC * 128.
+    // ---------------- epilogue: each sub-chunk into the float-pair tile(s) ----------------
+    // TMEM columns: buffer b holds [main][corr (exact scheme)] at b * NACC * NB.
     // The sub-chunk's sum (main exact, corr small) is unscaled by powers of two
     // and added with an error-free TwoSum into (hi, lo) in global memory, so the
     // running sum keeps about 48 bits with FP32 arithmetic only.
@@ -526,27 +530,29 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
     const float ia = 1.0f / sA_s[rl];       // exact: a power of two
     const int nt = a.ntile_side;
-    float2 *dst = a.Macc + (size_t)wk.w * a.slice + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb) * BN) * BM +
-                  rl;  // + col * BM
+    // column c of the accumulators: tile tb0 + c / BN, its column c mod BN
+    float2 *dst0 = a.Macc + (size_t)wk.w * a.slice + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb0) * BN) * BM + rl;
+    auto dst_of = [&](int c) { return dst0 + (size_t)(c / BN) * BN * BM + (size_t)(c % BN) * BM; };
     for (int sc = 0; sc < nsub; sc++) {
-      const int b = sc & 1;
-      if (!mbar_wait(&accfull[b], (sc >> 1) & 1, ab)) break;
+      const int b = sc % NBUF;
+      if (!mbar_wait(&accfull[b], (sc / NBUF) & 1, ab)) break;
       tc_fence_after();
-      const uint32_t base = lanebase + (uint32_t)(b * NACC * BN);
+      const uint32_t base = lanebase + (uint32_t)(b * NACC * NB);
       // the running sums of the next 8 columns are loaded while these 8 are
-      // added, so each step waits for one global round trip less
+      // added, so each step waits for one global round trip less (three groups
+      // in flight measured slower: register pressure)
       float2 g[8], gn[8] = {};
 #pragma unroll
-      for (int j = 0; j < 8; j++) g[j] = dst[(size_t)j * BM];
+      for (int j = 0; j < 8; j++) g[j] = dst_of(j)[0];
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 8) {
-        if (c0 + 8 < BN) {
+      for (int c0 = 0; c0 < NB; c0 += 8) {
+        if (c0 + 8 < NB) {
 #pragma unroll
-          for (int j = 0; j < 8; j++) gn[j] = dst[(size_t)(c0 + 8 + j) * BM];
+          for (int j = 0; j < 8; j++) gn[j] = dst_of(c0 + 8 + j)[0];
         }
         float m[8], cr[8];
         tmem_ld8(base + c0, m);
-        if (NACC == 2) tmem_ld8(base + BN + c0, cr);
+        if (NACC == 2) tmem_ld8(base + NB + c0, cr);
         tmem_wait_ld();
 #pragma unroll
         for (int j = 0; j < 8; j++) {
@@ -554,7 +560,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
           const float x = m[j] * f, l = (NACC == 2 ? cr[j] : 0.f) * f;
           const float sm = g[j].x + x, bb = sm - g[j].x;
           const float err = (g[j].x - (sm - bb)) + (x - bb);
-          dst[(size_t)(c0 + j) * BM] = make_float2(sm, g[j].y + err + l);
+          dst_of(c0 + j)[0] = make_float2(sm, g[j].y + err + l);
           g[j] = gn[j];
         }
       }
@@ -572,17 +578,17 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
           mbar_arrive_remote(rp0 + 8u * (uint32_t)s);
         }
       } else if (lane == 1) {
-        const uint32_t ra0 = cluster_addr(&paccempty[0], 0), ra1 = cluster_addr(&paccempty[1], 0);
-        // the issuer waits for the drains of sub-chunks 0 .. nsub - 3 only
-        for (int sc = 0; sc + 2 < nsub; sc++) {
-          const int b = sc & 1;
-          if (!mbar_wait(&accempty[b], (sc >> 1) & 1, ab)) break;
-          mbar_arrive_remote(b ? ra1 : ra0);
+        const uint32_t ra0 = cluster_addr(&paccempty[0], 0);  // paccempty[b] is ra0 + 8 b
+        // the issuer waits for the drains of sub-chunks 0 .. nsub - 1 - NBUF only
+        for (int sc = 0; sc + NBUF < nsub; sc++) {
+          const int b = sc % NBUF;
+          if (!mbar_wait(&accempty[b], (sc / NBUF) & 1, ab)) break;
+          mbar_arrive_remote(ra0 + 8u * (uint32_t)b);
         }
       }
     } else if (lane == 0) {
       // ---------------- MMA issuer ----------------
-      const uint32_t idesc = make_idesc(BF16 ? 1 : 0, PAIR ? 2 * BM : BM, BN);
+      const uint32_t idesc = make_idesc(BF16 ? 1 : 0, PAIR ? 2 * BM : BM, NB);
       // descriptors of every plane tile of stage 0, built once: per MMA the
       // issuing thread only adds the stage and the K step (32 bytes = 2 units of
       // the start address, which stays below 2^14 units), since it shares its
@@ -592,7 +598,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 #pragma unroll
       for (int p = 0; p < NP; p++) {
         dA[p] = make_desc(sb0 + (uint32_t)(AOFF + p * TILE_BYTES));
-        dB[p] = make_desc(sb0 + (uint32_t)(BOFF + p * BTILE));
+        dB[p] = make_desc(sb0 + (uint32_t)(BOFF + p * TILE_BYTES));
       }
       // the MMAs of one K block in stage s: products of planes pa (A) and pb (B)
       // with pa + pb <= NP - 1, grouped by A plane (collector reuse); with the
@@ -609,7 +615,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
             const uint64_t bd = dB[pb] + soff + (uint64_t)(2 * kk);
             constexpr bool main_acc = (EXACT && pa == 0 && pb == 0) || !EXACT;
             constexpr bool first = main_acc ? (pa == 0 && pb == 0) : (pa == 0 && pb == 1);
-            mma_plane<pb, NP - pa, CG>(main_acc ? tacc : tacc + BN, ad, bd, idesc, (first && fresh) ? 0 : 1);
+            mma_plane<pb, NP - pa, CG>(main_acc ? tacc : tacc + NB, ad, bd, idesc, (first && fresh) ? 0 : 1);
           };
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 0>{});
           prod(std::integral_constant<int, 0>{}, std::integral_constant<int, 1>{});
@@ -622,14 +628,15 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
         }
       };
       for (int sc = 0; sc < nsub && !ab.up(); sc++) {
-        // accumulator pair b; the epilogues must have drained it (sub-chunk sc - 2)
-        const int b = sc & 1;
-        if (sc >= 2) {
-          if (!mbar_wait(&accempty[b], ((sc - 2) >> 1) & 1, ab)) break;
-          if (PAIR && !mbar_wait<true>(&paccempty[b], ((sc - 2) >> 1) & 1, ab)) break;
+        // accumulator buffer b; the epilogues must have drained it (sub-chunk sc - NBUF)
+        const int b = sc % NBUF;
+        if (sc >= NBUF) {
+          const uint32_t par = ((sc - NBUF) / NBUF) & 1;
+          if (!mbar_wait(&accempty[b], par, ab)) break;
+          if (PAIR && !mbar_wait<true>(&paccempty[b], par, ab)) break;
         }
         tc_fence_after();
-        const uint32_t tacc = tmem + (uint32_t)(b * NACC * BN);
+        const uint32_t tacc = tmem + (uint32_t)(b * NACC * NB);
         const int kbeg = sc * ksub, kend = min(nkb, kbeg + ksub);
         bool ok = true;
         for (int kb = kbeg; kb < kend; kb++) {
@@ -652,7 +659,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     }
   } else if (lane == 0) {
     // ---------------- loader: B planes per K block, weights per chunk, by bulk copy ----------------
-    const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES + (size_t)rank * BTILE;
+    const unsigned char *bsrc = a.Bp + ((size_t)tb * nkb_all + kb0) * NP * TILE_BYTES;
     const float2 *wsrc = a.wt + (size_t)cidx * a.Kp + (size_t)kb0 * BK;
     const int nchunk = (nkb + WCH - 1) / WCH;
     auto issue_w = [&](int c) {
@@ -668,10 +675,10 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
       if (use > 0 && !mbar_wait(&empty[s], (use - 1) & 1, ab)) break;
       unsigned char *st = stage_base + (size_t)s * STAGE;
       if (kb + PF_AHEAD < nkb) bulk_prefetch_l2(bsrc + (size_t)(kb + PF_AHEAD) * NP * TILE_BYTES, NP * TILE_BYTES);
-      mbar_arrive_tx(&bfull[s], (uint32_t)(NP * BTILE));
+      mbar_arrive_tx(&bfull[s], (uint32_t)(NP * TILE_BYTES));
 #pragma unroll
       for (int p = 0; p < NP; p++)
-        bulk_g2s(st + BOFF + p * BTILE, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, BTILE, &bfull[s]);
+        bulk_g2s(st + BOFF + p * TILE_BYTES, bsrc + ((size_t)kb * NP + p) * TILE_BYTES, TILE_BYTES, &bfull[s]);
       issued = kb + 1;
       // chunk wnext reuses the slot of chunk wnext - 2 once the producers have left it
       if (wnext < nchunk && kb >= (wnext - 1) * WCH) {
@@ -880,16 +887,22 @@ static void *grow(void *&p, size_t &have, size_t need) {
 static int Gp_of(int ng) { return ((ng + BM - 1) / BM) * BM; }
 static int nplanes_of(int precision) { return (precision == RP_PREC_BF16X3 || precision == RP_PREC_FP16X3) ? 3 : 2; }
 static size_t smem_of(int precision, bool pair) {
-  // per stage: A planes, B planes (half a tile each in a CTA pair); the weight
-  // ring; then the barriers and the scales
+  // per stage: A planes, B planes; the weight ring; then the barriers and the
+  // row and column scales
   const size_t np = (size_t)nplanes_of(precision);
-  return 1024 + (size_t)nstage_of(pair) * np * (TILE_BYTES + (pair ? TILE_BYTES / 2 : TILE_BYTES)) +
-         2 * (size_t)wchunk_of(pair) * BK * 8 + 256 + 2 * sizeof(float) * BM;
+  return 1024 + (size_t)nstage_of(pair) * np * 2 * TILE_BYTES + 2 * (size_t)wchunk_of(pair) * BK * 8 + 256 +
+         sizeof(float) * (BM + (size_t)nb_of(pair));
 }
 static size_t slice_of(int Mp, int nen) { return (size_t)nen * 2 * Mp * Mp; }
-// K blocks per FP32 sub-chunk: 1024 K by default; the integer leading plane's
-// partial sums stay exact (below 2^24) only up to that length
-static int ksub_of(const TcWorkspace &ws) {
+// K blocks per FP32 sub-chunk: 1024 K by default, and at most that for the
+// 8-bit integer leading plane (its partial sums stay integers of at most
+// 2^24).  The tensor core's FP32 accumulation also loses accuracy in
+// proportion to the length of a sum (chi against the FP64 oracle, FP16x3 with
+// a 7-bit leading plane: 2.4e-7 at 256 K, 8.3e-7 at 1024 K, 3.4e-6 at 4096 K),
+// so longer sub-chunks would not pay even where the integers allowed them; a
+// CTA pair takes the same length.
+static int ksub_of(const TcWorkspace &ws, bool pair = false) {
+  (void)pair;
   const int k = ws.ksub > 0 ? ws.ksub : 16;
   return nplanes_of(ws.precision) == 3 ? std::min(k, 16) : k;
 }
@@ -1026,7 +1039,7 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
     const TcWorkspace &ws = *wss[i];
     TcArgs &a = probs[i];
     const int nt = ws.Mp / BM, nkb = ws.Kp / BK;
-    const int ksub = ksub_of(ws);
+    const int ksub = ksub_of(ws, P.pair);
     a.Yt = ws.Yt; a.sB = ws.sB; a.sA = ws.sA; a.wt = ws.wt; a.Bp = ws.Bp;
     a.Macc = (float2 *)ws.part;
     a.slice = slice_of(ws.Mp, ws.nen);
@@ -1035,14 +1048,16 @@ GroupPlan plan_group(TcWorkspace *const *wss, int n, cudaStream_t st, void *&dev
     const int nsp = (nkb + a.kb_split - 1) / a.kb_split;
     if (nsp > ws.nslice) fail(1, "tensor-core group: %d K splits for %d slices", nsp, ws.nslice);
     if (P.pair) {
-      // row tiles 2 tp and 2 tp + 1 against column tiles tb >= 2 tp, the pair's
-      // two CTAs adjacent (nt is even: Mp = 2 Gp); (2 tp + 1, 2 tp) is below
-      // the diagonal and never read
-      for (int tp = 0; tp < nt / 2; tp++)
-        for (int tb = 2 * tp; tb < nt; tb++)
+      // 2 x 2 blocks (tpa, tpb >= tpa) of tiles, the pair's two CTAs adjacent
+      // (nt is even: Mp = 2 Gp): CTA r takes row tile 2 tpa + r and loads
+      // column tile 2 tpb + r; tile (2 tpa + 1, 2 tpa) of a diagonal block is
+      // below the diagonal and never read
+      for (int tpa = 0; tpa < nt / 2; tpa++)
+        for (int tpb = tpa; tpb < nt / 2; tpb++)
           for (int sp = 0; sp < nsp; sp++)
             for (int c = 0; c < 2 * ws.nen; c++)
-              for (int r = 0; r < 2; r++) work.push_back(make_int4(i, (2 * tp + r) | (tb << 16), c, sp));
+              for (int r = 0; r < 2; r++)
+                work.push_back(make_int4(i, (2 * tpa + r) | ((2 * tpb + r) << 16), c, sp));
     } else {
       for (int ta = 0; ta < nt; ta++)
         for (int tb = ta; tb < nt; tb++)
