@@ -74,6 +74,7 @@ struct rp_ctx {
   // bands resident (slots 0..n_fixed-1), a window of nwin slots that each pair
   // batch fills with its virtual bands; h_slot_of / slot_of map band -> slot
   bool ur_window = false;
+  bool wfn_fp32 = false;  // the real-space transforms run in FP32 (split precisions)
   int n_fixed = 0, nwin = 0, nslot = 0;
   std::vector<int> h_slot_of;
   DevBuf slot_of, win_bands;
@@ -291,6 +292,10 @@ static void create_ctx(rp_ctx *c, const char *root, const rp_params *p, const do
   const size_t reserve = (size_t)48 << 30;
   const size_t avail = freeb > reserve ? freeb - reserve : 0;
   rp::WfnSlots sl;
+  // the split precisions transform in FP32 (then round to single, as both
+  // paths do); the FP64 precision and pair_fp64 keep the FP64 passes
+  sl.fp32 = p->precision != RP_PREC_FP64 && !p->pair_fp64;
+  c->wfn_fp32 = sl.fp32;
   if (p->ur_window > 0 || per_band * (size_t)S.ncb > avail) {
     c->ur_window = true;
     c->n_fixed = S.n_occ;
@@ -500,6 +505,7 @@ static void q_batch(rp_ctx *c, QRun &r, int bi, rp::TcWorkspace *ws, bool run_gr
     sl.slot_of = c->slot_of.as<int>();
     sl.nslot = c->nslot;
     sl.rotate = false;
+    sl.fp32 = c->wfn_fp32;
     c->launches += rp::launch_wfn_realspace(c->coef.as<double2>(), c->numirr.as<int>(), c->trs.as<int>(),
                                             c->src.as<int>(), c->phase.as<double2>(), c->ng0.as<int>(),
                                             c->kg0.as<int>(), S.ntk, S.ncb, S.ntg, n1, n2, n3, c->R[0], c->R[1],

@@ -78,13 +78,16 @@ template <typename K> inline int smem_cap(K kern) {
 // Which (k, band) real-space functions to make and where they go: bands (device
 // list of nbands absolute bands; null = every band), slot_of (device table band
 // -> slot, -1 = none; null = slot b with a stride of ncb bands), nslot (slots
-// per k), rotate (apply make_C0 to coef_irr and write cfull; false: read cfull).
+// per k), rotate (apply make_C0 to coef_irr and write cfull; false: read cfull),
+// fp32 (the transform's passes in FP32 instead of FP64; the rotation and cfull
+// stay FP64).
 struct WfnSlots {
   const int *bands = nullptr;
   int nbands = 0;
   const int *slot_of = nullptr;
   int nslot = 0;
   bool rotate = true;
+  bool fp32 = false;
 };
 int launch_wfn_realspace(const double2 *coef_irr, const int *numirr, const int *trs, const int *src,
                          const double2 *phase, const int *ng0, const int *kg0, int ntk, int ncb, int ntg,

@@ -16,6 +16,13 @@
 // time, staged in shared memory: the plane-wave sphere sits in a compact
 // (2R+1)^3 cube, so the z pass touches only the sphere's bounding box.
 //
+// The split precisions run the three passes in FP32 (WfnSlots::fp32): the
+// result is rounded to single either way, and a pass of at most n terms in
+// FP32 moves it by about a unit of that rounding, while GB300 runs FP32 at
+// many times its FP64 rate (the transform of every virtual band per pair batch
+// dominated the large workload's pair stage in FP64).  The FP64 precision and
+// pair_fp64 keep the FP64 passes.
+//
 // When the real-space functions of every band do not fit in HBM (1000 k x
 // 1000 bands on a 48^3 box would take 885 GB), the context keeps the occupied
 // bands resident and transforms each pair batch's virtual bands into a window
@@ -28,6 +35,7 @@ namespace rp {
 
 __device__ __forceinline__ int modp(int a, int n) { int m = a % n; return m < 0 ? m + n : m; }
 
+template <typename T>
 __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     const double2 *__restrict__ coef_irr, const int *__restrict__ numirr, const int *__restrict__ trs,
     const int *__restrict__ src, const double2 *__restrict__ phase, const int *__restrict__ ng0,
@@ -41,15 +49,18 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
   const size_t ur_at = (size_t)k * (sl.slot_of ? sl.nslot : ncb) + slot;
   const bool c1 = 2 * R1 + 1 <= n1, c2 = 2 * R2 + 1 <= n2, c3 = 2 * R3 + 1 <= n3;
   const int D1 = c1 ? 2 * R1 + 1 : n1, D2 = c2 ? 2 * R2 + 1 : n2, D3 = c3 ? 2 * R3 + 1 : n3;
-  double2 *cube = (double2 *)smem;                 // D1*D2*D3, index c1 + D1*(c2 + D2*c3)
-  double2 *A = cube + D1 * D2 * D3;                // D1*D2
-  double2 *B = A + D1 * D2;                        // D1*n2
-  double2 *tw1 = B + D1 * n2, *tw2 = tw1 + n1, *tw3 = tw2 + n2;
+  using T2 = typename C2<T>::t;
+  T2 *cube = (T2 *)smem;                           // D1*D2*D3, index c1 + D1*(c2 + D2*c3)
+  T2 *A = cube + D1 * D2 * D3;                     // D1*D2
+  T2 *B = A + D1 * D2;                             // D1*n2
+  T2 *tw1 = B + D1 * n2, *tw2 = tw1 + n1, *tw3 = tw2 + n2;
   int *f1 = (int *)(tw3 + n3), *f2 = f1 + D1, *f3 = f2 + D2;
-  for (int i = tid; i < D1 * D2 * D3; i += nt) cube[i] = make_double2(0, 0);
-  for (int j = tid; j < n1; j += nt) { double s, c; sincospi(2.0 * j / n1, &s, &c); tw1[j] = make_double2(c, s); }
-  for (int j = tid; j < n2; j += nt) { double s, c; sincospi(2.0 * j / n2, &s, &c); tw2[j] = make_double2(c, s); }
-  for (int j = tid; j < n3; j += nt) { double s, c; sincospi(2.0 * j / n3, &s, &c); tw3[j] = make_double2(c, s); }
+  const T2 zero = mk<T>(0, 0);
+  for (int i = tid; i < D1 * D2 * D3; i += nt) cube[i] = zero;
+  // twiddles from FP64 sincospi, rounded once to T
+  for (int j = tid; j < n1; j += nt) { double s, c; sincospi(2.0 * j / n1, &s, &c); tw1[j] = mk<T>((T)c, (T)s); }
+  for (int j = tid; j < n2; j += nt) { double s, c; sincospi(2.0 * j / n2, &s, &c); tw2[j] = mk<T>((T)c, (T)s); }
+  for (int j = tid; j < n3; j += nt) { double s, c; sincospi(2.0 * j / n3, &s, &c); tw3[j] = mk<T>((T)c, (T)s); }
   for (int j = tid; j < D1; j += nt) f1[j] = c1 ? modp(j - R1, n1) : j;
   for (int j = tid; j < D2; j += nt) f2[j] = c2 ? modp(j - R2, n2) : j;
   for (int j = tid; j < D3; j += nt) f3[j] = c3 ? modp(j - R3, n3) : j;
@@ -72,7 +83,7 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
       int i1 = c1 ? g[0] + R1 : modp(g[0], n1);
       int i2 = c2 ? g[1] + R2 : modp(g[1], n2);
       int i3 = c3 ? g[2] + R3 : modp(g[2], n3);
-      cube[i1 + D1 * (i2 + D2 * i3)] = v;
+      cube[i1 + D1 * (i2 + D2 * i3)] = mk<T>((T)v.x, (T)v.y);
     }
     if (sl.rotate) cf[ig] = v;
   }
@@ -82,9 +93,9 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
   for (int z = 0; z < n3; z++) {
     // pass z: A[c1,c2] = sum_c3 cube e^{+2 pi i f3 z / n3}
     for (int o = tid; o < D1 * D2; o += nt) {
-      double2 acc = make_double2(0, 0);
+      T2 acc = zero;
       for (int cc = 0; cc < D3; cc++) {
-        double2 v = cube[o + D1 * D2 * cc];
+        const T2 v = cube[o + D1 * D2 * cc];
         cfma(acc, v, tw3[(f3[cc] * z) % n3]);
       }
       A[o] = acc;
@@ -93,7 +104,7 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     // pass y: B[c1,y] = sum_c2 A e^{+2 pi i f2 y / n2}
     for (int o = tid; o < D1 * n2; o += nt) {
       int cc1 = o % D1, y = o / D1;
-      double2 acc = make_double2(0, 0);
+      T2 acc = zero;
       for (int cc = 0; cc < D2; cc++) cfma(acc, A[cc1 + D1 * cc], tw2[(f2[cc] * y) % n2]);
       B[o] = acc;
     }
@@ -101,7 +112,7 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     // pass x: u[x,y] = sum_c1 B e^{+2 pi i f1 x / n1}
     for (int o = tid; o < n1 * n2; o += nt) {
       int x = o % n1, y = o / n1;
-      double2 acc = make_double2(0, 0);
+      T2 acc = zero;
       for (int cc = 0; cc < D1; cc++) cfma(acc, B[cc + D1 * y], tw1[(f1[cc] * x) % n1]);
       out[(size_t)z * n1 * n2 + o] = make_float2((float)acc.x, (float)acc.y);
     }
@@ -118,14 +129,17 @@ int launch_wfn_realspace(const double2 *coef_irr, const int *numirr, const int *
   if (nb == 0 || k_end <= k_begin) return 0;
   const int D1 = 2 * R1 + 1 <= n1 ? 2 * R1 + 1 : n1, D2 = 2 * R2 + 1 <= n2 ? 2 * R2 + 1 : n2,
             D3 = 2 * R3 + 1 <= n3 ? 2 * R3 + 1 : n3;
-  size_t smem = sizeof(double2) * ((size_t)D1 * D2 * D3 + D1 * D2 + D1 * n2 + n1 + n2 + n3) +
-                sizeof(int) * (D1 + D2 + D3);
-  const int cap = smem_cap(wfn_realspace_kernel);
-  if (smem > (size_t)cap) fail(1, "plane-wave sphere too large for the shared-memory cube (%zu bytes)", smem);
-  RP_CUDA(cudaFuncSetAttribute(wfn_realspace_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
-  dim3 grid(nb, k_end - k_begin);
-  wfn_realspace_kernel<<<grid, 256, smem, st>>>(coef_irr, numirr, trs, src, phase, ng0, kg0, ncb, ntg, n1, n2,
-                                                n3, R1, R2, R3, cfull, ur, k_begin, sl);
+  auto run = [&](auto kern, size_t cplx) {
+    const size_t smem = cplx * ((size_t)D1 * D2 * D3 + D1 * D2 + D1 * n2 + n1 + n2 + n3) + sizeof(int) * (D1 + D2 + D3);
+    const int cap = smem_cap(kern);
+    if (smem > (size_t)cap) fail(1, "plane-wave sphere too large for the shared-memory cube (%zu bytes)", smem);
+    RP_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    dim3 grid(nb, k_end - k_begin);
+    kern<<<grid, 256, smem, st>>>(coef_irr, numirr, trs, src, phase, ng0, kg0, ncb, ntg, n1, n2, n3, R1, R2, R3, cfull,
+                                  ur, k_begin, sl);
+  };
+  if (sl.fp32) run(wfn_realspace_kernel<float>, sizeof(float2));
+  else run(wfn_realspace_kernel<double>, sizeof(double2));
   RP_CUDA(cudaGetLastError());
   return 1;
 }
