@@ -365,6 +365,67 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                : "memory");
 }
 
+// A warp's view of the accumulator drain: its 32 rows of the float-pair tile(s)
+// in global memory, the column scales, its row scale, its tensor-memory lanes.
+struct DrainCtx {
+  float2 *dst0;      // row rl of column 0 of the first tile; column c at (c / BN) BN BM + (c mod BN) BM
+  const float *rB;   // 1 / column scales (NB)
+  float ia;          // 1 / row scale
+  uint32_t base;     // tensor memory: this warp's lane quarter, column 0
+  uint64_t *accfull, *accempty;
+  Abort ab;
+};
+
+// Drains sub-chunk sc: TMEM columns of buffer b hold [main][corr (exact
+// scheme)] at b * NACC * NB.  The sub-chunk's sum (main exact, corr small) is
+// unscaled by powers of two and added with an error-free TwoSum into (hi, lo)
+// in global memory, so the running sum keeps about 48 bits with FP32
+// arithmetic only.  Worker j of the W warps of a lane quarter takes the
+// 8-column groups j, j + W, ...; the running sums of its next group are loaded
+// while this one is added.
+template <int NB, int NBUF, int NACC>
+__device__ __forceinline__ bool drain_body(const DrainCtx &dc, int sc, int j, int W) {
+  const int b = sc % NBUF;
+  if (!mbar_wait(&dc.accfull[b], (sc / NBUF) & 1, dc.ab)) return false;
+  tc_fence_after();
+  auto dst_of = [&](int c) { return dc.dst0 + (size_t)(c / BN) * BN * BM + (size_t)(c % BN) * BM; };
+  const uint32_t base = dc.base + (uint32_t)(b * NACC * NB);
+  float2 g[8], gn[8] = {};
+  if (8 * j < NB) {
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) g[jj] = dst_of(8 * j + jj)[0];
+  }
+#pragma unroll 1
+  for (int c0 = 8 * j; c0 < NB; c0 += 8 * W) {
+    if (c0 + 8 * W < NB) {
+#pragma unroll
+      for (int jj = 0; jj < 8; jj++) gn[jj] = dst_of(c0 + 8 * W + jj)[0];
+    }
+    float m[8], cr[8];
+    tmem_ld8(base + c0, m);
+    if (NACC == 2) tmem_ld8(base + NB + c0, cr);
+    tmem_wait_ld();
+#pragma unroll
+    for (int jj = 0; jj < 8; jj++) {
+      const float f = dc.ia * dc.rB[c0 + jj];
+      const float x = m[jj] * f, l = (NACC == 2 ? cr[jj] : 0.f) * f;
+      const float sm = g[jj].x + x, bb = sm - g[jj].x;
+      const float err = (g[jj].x - (sm - bb)) + (x - bb);
+      dst_of(c0 + jj)[0] = make_float2(sm, g[jj].y + err + l);
+      g[jj] = gn[jj];
+    }
+  }
+  tc_fence_before();
+  mbar_arrive(&dc.accempty[b]);
+  return true;
+}
+// out of line, for the producer warps that help drain in a CTA pair: they keep
+// their registers for the production loop
+template <int NB, int NBUF, int NACC>
+__device__ __noinline__ bool drain_sub(const DrainCtx &dc, int sc, int j, int W) {
+  return drain_body<NB, NBUF, NACC>(dc, sc, j, W);
+}
+
 // NP operand planes, EXACT integer leading plane, BF16 or FP16.  One CTA per
 // work item (problem, upper tile, frequency, Re/Im weight, K split); see the
 // file comment for the roles.
@@ -391,6 +452,10 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
   constexpr int NST = nstage_of(PAIR), WCH = wchunk_of(PAIR), WB = WCH * BK * 8;
   constexpr int NB = nb_of(PAIR), NBUF = nbuf_of(PAIR);  // accumulator columns, buffers
+  // warps that drain the accumulators: the epilogue warps, and in a CTA pair,
+  // whose single-buffered MMAs wait for every drain, the producer warps too
+  // (five warps per tensor-memory lane quarter)
+  constexpr int DRAIN_THREADS = PAIR ? NEPI + NPROD : NEPI, DRAIN_W = DRAIN_THREADS / NEPI;
   constexpr int AOFF = 0, BOFF = NP * TILE_BYTES;
   constexpr int STAGE = 2 * NP * TILE_BYTES;        // A planes, B planes
   unsigned char *stage_base = smem;
@@ -433,7 +498,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(&accfull[b], 1);
-      mbar_init(&accempty[b], NEPI);
+      mbar_init(&accempty[b], DRAIN_THREADS);
       mbar_init(&paccempty[b], 1);
       mbar_init(&wready[b], 1);
       mbar_init(&wfree[b], NPROD);
@@ -468,6 +533,23 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   for (int i = tid; i < NB; i += NTHREADS) rB_s[i] = 1.0f / a.sB[tb0 * BN + i];  // exact: a power of two
   __syncthreads();
 
+  // ---------------- draining a sub-chunk into the float-pair tile(s) ----------------
+  // (drain_sub below; its state is fixed per warp)
+  DrainCtx dc;
+  {
+    const int qd = warp & 3, rl = 32 * qd + lane;  // row within the tile
+    const int nt = a.ntile_side;
+    dc.dst0 = a.Macc + (size_t)wk.w * a.slice + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb0) * BN) * BM + rl;
+    dc.rB = rB_s;
+    dc.ia = 1.0f / sA_s[rl];  // exact: a power of two
+    dc.base = tmem + ((uint32_t)(32 * qd) << 16);
+    dc.accfull = accfull;
+    dc.accempty = accempty;
+    dc.ab = ab;
+  }
+  auto drain = [&](int sc, int j, int W) { return drain_sub<NB, NBUF, NACC>(dc, sc, j, W); };
+  auto drain_inline = [&](int sc, int j, int W) { return drain_body<NB, NBUF, NACC>(dc, sc, j, W); };
+
   if (warp < NPROD / 32) {
     // ---------------- producers: the weighted A operand ----------------
     // warp pw owns rows PROWS pw .. PROWS (pw + 1) - 1; lane l the K pair 2l, 2l+1 of every
@@ -481,8 +563,19 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 #pragma unroll
     for (int i = 0; i < PROWS; i++) cur[i] = __ldg(ya + i * rstride);
     const uint32_t cofs = (uint32_t)(lane & 3) * 4, chunk = (uint32_t)(lane >> 2);
+    int drained = 0;  // sub-chunks this warp has helped drain (CTA pairs)
+    bool ok = true;
     for (int kb = 0; kb < nkb; kb++) {
       const int s = kb % NST, use = kb / NST;
+      // CTA pairs: before waiting for the stage of block kb, whose MMAs of block
+      // kb - NST run only once every sub-chunk before that block's is drained,
+      // help drain those (their MMAs have all been issued: their blocks are
+      // produced)
+      if (PAIR && kb >= NST) {
+        const int target = (kb - NST) / ksub;
+        for (; ok && drained < target; drained++) ok = drain(drained, 1 + warp / 4, DRAIN_W);
+        if (!ok) break;
+      }
       if (kb + 1 < nkb) {
 #pragma unroll
         for (int i = 0; i < PROWS; i++) nxt[i] = __ldg(ya + i * rstride + (size_t)(kb + 1) * (BK / 2));
@@ -519,54 +612,14 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 #pragma unroll
       for (int i = 0; i < PROWS; i++) cur[i] = nxt[i];
     }
+    // the sub-chunks not drained inside the loop (at least the last)
+    if (PAIR && ok)
+      for (; drained < nsub; drained++)
+        if (!drain(drained, 1 + warp / 4, DRAIN_W)) break;
   } else if (warp < MMA_WARP) {
-    // ---------------- epilogue: each sub-chunk into the float-pair tile(s) ----------------
-    // TMEM columns: buffer b holds [main][corr (exact scheme)] at b * NACC * NB.
-    // The sub-chunk's sum (main exact, corr small) is unscaled by powers of two
-    // and added with an error-free TwoSum into (hi, lo) in global memory, so the
-    // running sum keeps about 48 bits with FP32 arithmetic only.
-    const int q = warp & 3;                 // this warp may read TMEM lanes 32q..32q+31
-    const int rl = 32 * q + lane;           // row within the tile
-    const uint32_t lanebase = tmem + ((uint32_t)(32 * q) << 16);
-    const float ia = 1.0f / sA_s[rl];       // exact: a power of two
-    const int nt = a.ntile_side;
-    // column c of the accumulators: tile tb0 + c / BN, its column c mod BN
-    float2 *dst0 = a.Macc + (size_t)wk.w * a.slice + (((((size_t)e * 2 + ch) * nt + ta) * nt + tb0) * BN) * BM + rl;
-    auto dst_of = [&](int c) { return dst0 + (size_t)(c / BN) * BN * BM + (size_t)(c % BN) * BM; };
-    for (int sc = 0; sc < nsub; sc++) {
-      const int b = sc % NBUF;
-      if (!mbar_wait(&accfull[b], (sc / NBUF) & 1, ab)) break;
-      tc_fence_after();
-      const uint32_t base = lanebase + (uint32_t)(b * NACC * NB);
-      // the running sums of the next 8 columns are loaded while these 8 are
-      // added, so each step waits for one global round trip less (three groups
-      // in flight measured slower: register pressure)
-      float2 g[8], gn[8] = {};
-#pragma unroll
-      for (int j = 0; j < 8; j++) g[j] = dst_of(j)[0];
-#pragma unroll 1
-      for (int c0 = 0; c0 < NB; c0 += 8) {
-        if (c0 + 8 < NB) {
-#pragma unroll
-          for (int j = 0; j < 8; j++) gn[j] = dst_of(c0 + 8 + j)[0];
-        }
-        float m[8], cr[8];
-        tmem_ld8(base + c0, m);
-        if (NACC == 2) tmem_ld8(base + NB + c0, cr);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const float f = ia * rB_s[c0 + j];
-          const float x = m[j] * f, l = (NACC == 2 ? cr[j] : 0.f) * f;
-          const float sm = g[j].x + x, bb = sm - g[j].x;
-          const float err = (g[j].x - (sm - bb)) + (x - bb);
-          dst_of(c0 + j)[0] = make_float2(sm, g[j].y + err + l);
-          g[j] = gn[j];
-        }
-      }
-      tc_fence_before();
-      mbar_arrive(&accempty[b]);
-    }
+    // ---------------- epilogue: every sub-chunk into the float-pair tile(s) ----------------
+    for (int sc = 0; sc < nsub; sc++)
+      if (!drain_inline(sc, 0, DRAIN_W)) break;
   } else if (warp == MMA_WARP) {
     if (PAIR && rank == 1) {
       // ---------------- the second CTA of a pair: relays to the issuer ----------------
