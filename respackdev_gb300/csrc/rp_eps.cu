@@ -80,7 +80,7 @@ __device__ __forceinline__ typename C2<T>::t crecip(typename C2<T>::t b) {
 // of the unit vector e_{P_t} under the b steps, and every column x transforms
 // as x <- x - (E_P - Pan) x_P, i.e.
 //   A[:,T] <- (A[:,T] with rows P zeroed) + Pan A_old[P,T]
-// (gj_trail_kernel, A_old[P,T] copied by the panel kernel before the update).
+// (gj_trail_kernel, A_old[P,T] copied by gj_prows_kernel before the update).
 // Per element the same operations as the one-step-at-a-time elimination up to
 // the order of the b-term sums; the matrices are read and written once per
 // panel instead of once per pivot.
@@ -88,7 +88,7 @@ __device__ __forceinline__ typename C2<T>::t crecip(typename C2<T>::t b) {
 // widest panel: 32 columns in FP32, 16 in FP64 (the trailing update's 64-row
 // tiles of the panel and the pivot rows stay within 32 KB of shared memory)
 template <typename T>
-constexpr int panel_max() { return sizeof(T) == 4 ? 32 : 16; }
+__host__ __device__ constexpr int panel_max() { return sizeof(T) == 4 ? 32 : 16; }
 
 // panel width for n: the panel (b columns), the scaled pivot column and the
 // row flags in shared memory
@@ -118,10 +118,8 @@ __global__ void __launch_bounds__(512) gj_panel_kernel(typename C2<T>::t *__rest
   __shared__ int si[32];
   __shared__ T2 prow[panel_max<T>()], sd;
   __shared__ int sp;
-  for (size_t l = tid; l < (size_t)b * n; l += nth) {
-    const int i = (int)(l % n), t = (int)(l / n);
-    pan[l] = Am[i + (size_t)n * (k0 + t)];
-  }
+  for (int t = 0; t < b; t++)
+    for (int i = tid; i < n; i += nth) pan[(size_t)t * n + i] = Am[i + (size_t)n * (k0 + t)];
   for (int i = tid; i < n; i += nth) us[i] = um[i];
   __syncthreads();
   for (int t = 0; t < b; t++) {
@@ -161,34 +159,47 @@ __global__ void __launch_bounds__(512) gj_panel_kernel(typename C2<T>::t *__rest
     if (tid < b) prow[tid] = pan[(size_t)tid * n + p];
     for (int i = tid; i < n; i += nth) fc[i] = cmul(pan[(size_t)t * n + i], d);
     __syncthreads();
-    for (size_t l = tid; l < (size_t)b * n; l += nth) {
-      const int i = (int)(l % n), j = (int)(l / n);
-      T2 &a = pan[l];
-      const T2 pj = prow[j];
-      if (i == p) {
-        a = (j == t) ? d : cmul(pj, d);
-      } else if (j == t) {
-        a = mk<T>(-fc[i].x, -fc[i].y);
-      } else {
-        const T2 f = fc[i];
-        a.x = fma(-f.x, pj.x, a.x); a.x = fma(f.y, pj.y, a.x);
-        a.y = fma(-f.x, pj.y, a.y); a.y = fma(-f.y, pj.x, a.y);
+    // columns outer, rows inner (no index division); a thread keeps its rows'
+    // scaled pivot-column values in registers across the columns
+    for (int i0 = 0; i0 < n; i0 += nth) {
+      const int i = i0 + tid;
+      if (i >= n) continue;
+      const T2 f = fc[i];
+      for (int j = 0; j < b; j++) {
+        T2 &a = pan[(size_t)j * n + i];
+        const T2 pj = prow[j];
+        if (i == p) {
+          a = (j == t) ? d : cmul(pj, d);
+        } else if (j == t) {
+          a = mk<T>(-f.x, -f.y);
+        } else {
+          a.x = fma(-f.x, pj.x, a.x); a.x = fma(f.y, pj.y, a.x);
+          a.y = fma(-f.x, pj.y, a.y); a.y = fma(-f.y, pj.x, a.y);
+        }
       }
     }
     __syncthreads();
   }
-  for (size_t l = tid; l < (size_t)b * n; l += nth) {
-    const int i = (int)(l % n), t = (int)(l / n);
-    Am[i + (size_t)n * (k0 + t)] = pan[l];
-  }
+  for (int t = 0; t < b; t++)
+    for (int i = tid; i < n; i += nth) Am[i + (size_t)n * (k0 + t)] = pan[(size_t)t * n + i];
   for (int i = tid; i < n; i += nth) um[i] = us[i];
-  // the pivot rows outside the panel, before the trailing update: prows[m][t][j]
-  T2 *pr = prows + (size_t)m * b * n;
-  for (size_t l = tid; l < (size_t)b * n; l += nth) {
-    const int j = (int)(l % n), t = (int)(l / n);
-    if (j >= k0 && j < k0 + b) continue;
-    pr[l] = Am[pm[k0 + t] + (size_t)n * j];
-  }
+}
+
+// The panel's pivot rows outside the panel, before the trailing update:
+// prows[m][t][j] = A[P_t, j].  Row reads of column-major matrices are one
+// sector per element, so they run as their own grid (matrix, panel column)
+// for the memory parallelism.
+template <typename T>
+__global__ void __launch_bounds__(256) gj_prows_kernel(const typename C2<T>::t *__restrict__ A, int n, int k0, int b,
+                                                       const int *__restrict__ piv,
+                                                       typename C2<T>::t *__restrict__ prows) {
+  const int t = blockIdx.x, m = blockIdx.y;
+  const size_t nn = (size_t)n * n;
+  const int p = piv[(size_t)m * n + k0 + t];
+  const typename C2<T>::t *Am = A + m * nn;
+  typename C2<T>::t *pr = prows + ((size_t)m * b + t) * n;
+  for (int j = threadIdx.x; j < n; j += blockDim.x)
+    if (j < k0 || j >= k0 + b) pr[j] = Am[p + (size_t)n * j];
 }
 
 constexpr int TT = 64;  // trailing-update tile (TT x TT per CTA, 4 x 4 per thread)
@@ -297,8 +308,9 @@ static int blocked_gauss_jordan(typename C2<T>::t *A, int n, int nmat, typename 
   for (int k0 = 0; k0 < n; k0 += bw) {
     const int b = std::min(bw, n - k0);
     gj_panel_kernel<T><<<nmat, 512, psmem, st>>>(A, n, k0, b, piv, used, prows, err);
+    gj_prows_kernel<T><<<dim3(b, nmat), 256, 0, st>>>(A, n, k0, b, piv, prows);
     gj_trail_kernel<T><<<tgrid, 256, 0, st>>>(A, n, k0, b, piv, prows);
-    launches += 2;
+    launches += 3;
   }
   RP_CUDA(cudaGetLastError());
   // `used` doubles as the inverse-permutation scratch of the unscramble step
