@@ -91,12 +91,18 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
   __syncthreads();
   float2 *out = ur + ur_at * (size_t)n1 * n2 * n3;
   for (int z = 0; z < n3; z++) {
-    // pass z: A[c1,c2] = sum_c3 cube e^{+2 pi i f3 z / n3}
+    // pass z: A[c1,c2] = sum_c3 cube e^{+2 pi i f3 z / n3}.  The frequencies f
+    // of consecutive c are consecutive mod n, so the twiddle index f z mod n
+    // steps by z: one modulo per sum instead of one per term (all passes).
+    const int z0 = (f3[0] * z) % n3;
     for (int o = tid; o < D1 * D2; o += nt) {
       T2 acc = zero;
+      int ix = z0;
       for (int cc = 0; cc < D3; cc++) {
         const T2 v = cube[o + D1 * D2 * cc];
-        cfma(acc, v, tw3[(f3[cc] * z) % n3]);
+        cfma(acc, v, tw3[ix]);
+        ix += z;
+        if (ix >= n3) ix -= n3;
       }
       A[o] = acc;
     }
@@ -105,7 +111,12 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     for (int o = tid; o < D1 * n2; o += nt) {
       int cc1 = o % D1, y = o / D1;
       T2 acc = zero;
-      for (int cc = 0; cc < D2; cc++) cfma(acc, A[cc1 + D1 * cc], tw2[(f2[cc] * y) % n2]);
+      int ix = (f2[0] * y) % n2;
+      for (int cc = 0; cc < D2; cc++) {
+        cfma(acc, A[cc1 + D1 * cc], tw2[ix]);
+        ix += y;
+        if (ix >= n2) ix -= n2;
+      }
       B[o] = acc;
     }
     __syncthreads();
@@ -113,7 +124,12 @@ __global__ void __launch_bounds__(256) wfn_realspace_kernel(
     for (int o = tid; o < n1 * n2; o += nt) {
       int x = o % n1, y = o / n1;
       T2 acc = zero;
-      for (int cc = 0; cc < D1; cc++) cfma(acc, B[cc + D1 * y], tw1[(f1[cc] * x) % n1]);
+      int ix = (f1[0] * x) % n1;
+      for (int cc = 0; cc < D1; cc++) {
+        cfma(acc, B[cc + D1 * y], tw1[ix]);
+        ix += x;
+        if (ix >= n1) ix -= n1;
+      }
       out[(size_t)z * n1 * n2 + o] = make_float2((float)acc.x, (float)acc.y);
     }
     __syncthreads();
