@@ -766,22 +766,64 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
 // helpers: transpose the batch's pair densities and weights into the GEMM's
 // K-major operands, batch maxima, Gamma rows/columns, final assembly.
 
+__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
+  atomicMax((int *)addr, __float_as_int(v));  // valid for non-negative floats
+}
+
 // Yt[g][K] = Re rho, Yt[Gp+g][K] = Im rho, K = k*npair + p (rho is [p][k][g],
-// float2 or, with FP64 pair densities, double2 rounded to float as chiqw_sub.F:201)
+// float2 or, with FP64 pair densities, double2 rounded to float as chiqw_sub.F:201),
+// and the rows' maxima over K (rowmax, zeroed beforehand).  A tiled transpose:
+// a CTA reads 32 K x 64 g coalesced along g, keeps the tile in shared memory
+// and writes 64 rows of 32 consecutive K (128-byte segments).
+constexpr int YT_K = 32, YT_G = 64;
 template <typename R>
-__global__ void yt_kernel(const R *__restrict__ rho, int npair, int ntk, int ng, int Gp, int Kp,
-                          float *__restrict__ Yt, const double2 *__restrict__ head, int g0) {
-  const long K = (long)blockIdx.x;  // one K per block
-  const int k = (int)(K / npair), p = (int)(K % npair);
-  const R *src = rho + ((size_t)p * ntk + k) * ng;
-  for (int g = threadIdx.x; g < ng; g += blockDim.x) {
-    float2 v = make_float2((float)src[g].x, (float)src[g].y);
-    if (head && g == g0) {
-      double2 h = head[((size_t)p * ntk + k) * 3];
-      v = make_float2((float)h.x, (float)h.y);
+__global__ void __launch_bounds__(256) yt_kernel(const R *__restrict__ rho, int npair, int ntk, int ng, int Gp, int Kp,
+                                                 long Kn, float *__restrict__ Yt, const double2 *__restrict__ head,
+                                                 int g0, float *__restrict__ rowmax) {
+  __shared__ float2 tile[YT_G][YT_K + 1];
+  const long K0 = (long)blockIdx.x * YT_K;
+  const int gb = blockIdx.y * YT_G, tid = threadIdx.x;
+  // load: thread (g = tid mod 64, K rows tid / 64, +4, ...)
+  {
+    const int gl = tid & (YT_G - 1), g = gb + gl;
+    for (int kk = tid >> 6; kk < YT_K; kk += 256 / YT_G) {
+      const long K = K0 + kk;
+      float2 v = make_float2(0.f, 0.f);
+      if (K < Kn && g < ng) {
+        const int k = (int)(K / npair), p = (int)(K % npair);
+        const R x = rho[((size_t)p * ntk + k) * ng + g];
+        v = make_float2((float)x.x, (float)x.y);
+        if (head && g == g0) {
+          const double2 h = head[((size_t)p * ntk + k) * 3];
+          v = make_float2((float)h.x, (float)h.y);
+        }
+      }
+      tile[gl][kk] = v;
     }
-    Yt[(size_t)g * Kp + K] = v.x;
-    Yt[(size_t)(Gp + g) * Kp + K] = v.y;
+  }
+  __syncthreads();
+  // store: a warp writes 32 consecutive K of one row (Re, then Im); lane 0 keeps the row's maxima
+  const int kk = tid & (YT_K - 1);
+  for (int gl = tid >> 5; gl < YT_G; gl += 256 / YT_K) {
+    const int g = gb + gl;
+    if (g >= ng) break;
+    const long K = K0 + kk;
+    const float2 v = tile[gl][kk];
+    float mr = 0.f, mi = 0.f;
+    if (K < Kn) {
+      Yt[(size_t)g * Kp + K] = v.x;
+      Yt[(size_t)(Gp + g) * Kp + K] = v.y;
+      mr = fabsf(v.x);
+      mi = fabsf(v.y);
+    }
+    for (int o = 16; o; o >>= 1) {
+      mr = fmaxf(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+      mi = fmaxf(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    }
+    if (kk == 0) {
+      atomic_max_pos(&rowmax[g], mr);
+      atomic_max_pos(&rowmax[Gp + g], mi);
+    }
   }
 }
 
@@ -798,17 +840,9 @@ __global__ void wt_kernel(const double2 *__restrict__ w, int npair, int ntk, int
   }
 }
 
-__device__ __forceinline__ void atomic_max_pos(float *addr, float v) {
-  atomicMax((int *)addr, __float_as_int(v));  // valid for non-negative floats
-}
 
-__global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const float2 *__restrict__ wt, int nen, int Kp,
-                             long Kn, float *__restrict__ out) {
-  float m = 0.f;
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < nY; i += (size_t)gridDim.x * blockDim.x)
-    m = fmaxf(m, fabsf(Yt[i]));
-  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomic_max_pos(&out[0], m);
+// per-channel maxima of the weights (hi words) over the batch's K: out[1 + c]
+__global__ void maxes_kernel(const float2 *__restrict__ wt, int nen, int Kp, long Kn, float *__restrict__ out) {
   for (int e = 0; e < nen; e++) {
     float mr = 0.f, mi = 0.f;
     for (long K = (long)blockIdx.x * blockDim.x + threadIdx.x; K < Kn; K += (long)gridDim.x * blockDim.x) {
@@ -820,21 +854,6 @@ __global__ void maxes_kernel(const float *__restrict__ Yt, size_t nY, const floa
       mi = fmaxf(mi, __shfl_xor_sync(0xffffffffu, mi, o));
     }
     if ((threadIdx.x & 31) == 0) { atomic_max_pos(&out[1 + 2 * e], mr); atomic_max_pos(&out[2 + 2 * e], mi); }
-  }
-}
-
-// per-row maxima of Yt over the batch's K
-__global__ void rowmax_kernel(const float *__restrict__ Yt, int Kp, long Kn, float *__restrict__ rowmax) {
-  const float *r = Yt + (size_t)blockIdx.x * Kp;
-  float m = 0.f;
-  for (long K = threadIdx.x; K < Kn; K += blockDim.x) m = fmaxf(m, fabsf(r[K]));
-  for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  __shared__ float sm[32];
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int i = 1; i < (int)(blockDim.x >> 5); i++) m = fmaxf(m, sm[i]);
-    rowmax[blockIdx.x] = fmaxf(m, sm[0]);
   }
 }
 
@@ -1278,14 +1297,17 @@ int tc_prepare(TcWorkspace &ws, const float2 *rho, const double2 *rho64, const d
   unsigned char *Bp = base + sboff;
   RP_CUDA(cudaMemsetAsync(base, 0, ybytes + wbytes + mxbytes, st));
   if (Kn > 0x7fffffffL) fail(1, "batch too large");
-  if (rho64) yt_kernel<double2><<<(unsigned)Kn, 128, 0, st>>>(rho64, npair, ntk, ng, Gp, Kp, Yt, head, g0);
-  else yt_kernel<float2><<<(unsigned)Kn, 128, 0, st>>>(rho, npair, ntk, ng, Gp, Kp, Yt, head, g0);
+  RP_CUDA(cudaMemsetAsync(rowmax, 0, sizeof(float) * (size_t)Mp, st));
+  {
+    const dim3 g((unsigned)((Kn + YT_K - 1) / YT_K), (unsigned)((ng + YT_G - 1) / YT_G));
+    if (rho64) yt_kernel<double2><<<g, 256, 0, st>>>(rho64, npair, ntk, ng, Gp, Kp, Kn, Yt, head, g0, rowmax);
+    else yt_kernel<float2><<<g, 256, 0, st>>>(rho, npair, ntk, ng, Gp, Kp, Kn, Yt, head, g0, rowmax);
+  }
   wt_kernel<<<(unsigned)((Kn + 255) / 256), 256, 0, st>>>(w, npair, ntk, nen, Kp, wt);
-  maxes_kernel<<<1024, 256, 0, st>>>(Yt, (size_t)Mp * Kp, wt, nen, Kp, Kn, maxes);
-  rowmax_kernel<<<Mp, 256, 0, st>>>(Yt, Kp, Kn, rowmax);
+  maxes_kernel<<<1024, 256, 0, st>>>(wt, nen, Kp, Kn, maxes);
   const int exact = nplanes == 3 ? 1 : 0;
   scales_kernel<<<(Mp + 127) / 128, 128, 0, st>>>(rowmax, maxes, Mp, nen, exact ? 7 : 14, sBv, sAv);
-  launches += 5;
+  launches += 4;
   RP_CUDA(cudaGetLastError());
   if (head && rowcol && !rho64) {
     dim3 g(ng, nen, 2);
