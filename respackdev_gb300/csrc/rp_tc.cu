@@ -74,8 +74,6 @@ constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
 constexpr int WCHUNK = 16;                 // K blocks per weight chunk
 // stages and weight chunk of a kernel variant
-__host__ __device__ constexpr int nstage_of(bool) { return NSTAGE; }
-__host__ __device__ constexpr int wchunk_of(bool) { return WCHUNK; }
 // accumulator columns of a CTA (a CTA pair: both column tiles of its 2 x 2
 // block) and tensor-memory buffers of them (a pair: one, its two accumulators
 // of 256 columns fill the 512)
@@ -450,7 +448,7 @@ __global__ void __maxnreg__(80) tc_gram_kernel(TcGroup grp) {
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   constexpr int CG = PAIR ? 2 : 1;
   constexpr int NACC = EXACT ? 2 : 1;               // accumulators
-  constexpr int NST = nstage_of(PAIR), WCH = wchunk_of(PAIR), WB = WCH * BK * 8;
+  constexpr int NST = NSTAGE, WCH = WCHUNK, WB = WCH * BK * 8;
   constexpr int NB = nb_of(PAIR), NBUF = nbuf_of(PAIR);  // accumulator columns, buffers
   // warps that drain the accumulators: the epilogue warps, and in a CTA pair,
   // whose single-buffered MMAs wait for every drain, the producer warps too
@@ -962,7 +960,7 @@ static size_t smem_of(int precision, bool pair) {
   // per stage: A planes, B planes; the weight ring; then the barriers and the
   // row and column scales
   const size_t np = (size_t)nplanes_of(precision);
-  return 1024 + (size_t)nstage_of(pair) * np * 2 * TILE_BYTES + 2 * (size_t)wchunk_of(pair) * BK * 8 + 256 +
+  return 1024 + (size_t)NSTAGE * np * 2 * TILE_BYTES + 2 * (size_t)WCHUNK * BK * 8 + 256 +
          sizeof(float) * (BM + (size_t)nb_of(pair));
 }
 static size_t slice_of(int Mp, int nen) { return (size_t)nen * 2 * Mp * Mp; }
