@@ -73,7 +73,6 @@ constexpr int PROWS = BM / (NPROD / 32); // A rows per producer warp
 constexpr int MMA_WARP = (NPROD + NEPI) / 32;
 constexpr int NTHREADS = NPROD + NEPI + 64;
 constexpr int WCHUNK = 16;                 // K blocks per weight chunk
-// stages and weight chunk of a kernel variant
 // accumulator columns of a CTA (a CTA pair: both column tiles of its 2 x 2
 // block) and tensor-memory buffers of them (a pair: one, its two accumulators
 // of 256 columns fill the 512)
