@@ -157,8 +157,8 @@ int rp_chi0_q(rp_ctx *ctx, int iq, double *chi, int *ng_out, int *ndir_out);
 int rp_chi0_batch(rp_ctx *const *ctxs, const int *iqs, int n, int use_graph, double *const *chi, int *ng_out,
                   int *ndir_out, double *seconds);
 
-/* K-split shapes the tensor-core split tuner has measured in this process,
- * and a reset of its cache (for tests). */
+/* Shapes (K split and CTA shape) the tensor-core launch tuner has measured in
+ * this process, and a reset of its cache (for tests). */
 int rp_tuned_shapes(void);
 void rp_reset_tuner(void);
 

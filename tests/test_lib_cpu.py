@@ -45,10 +45,13 @@ def test_namelist_parser():
  1 2
  5
  &param_gpu precision='bf16x3', fft_box = 24, 24, 24, freq_re_ev=0.0,2.0 freq_im_ev=0.0,0.5,
-  tc_split=4, pair_batch=100, write_eps_f32=1 /
+  tc_split=4, pair_batch=100, write_eps_f32=1, tc_pair=2, tetra_fp64=1, ur_window=3, eps_fp64=1,
+  tail_model='net.bin' /
 """
     p, q, em = rp.parse_namelist(text)
     assert p.tc_split == 4 and p.pair_batch == 100 and p.write_eps_f32 == 1
+    assert p.tc_pair == 2 and p.tetra_fp64 == 1 and p.ur_window == 3 and p.eps_fp64 == 1
+    assert p.tail_model == b"net.bin"
     assert p.n_calc_band == 40 and p.flg_crpa == 1 and p.flg_calc_type == 2 and p.mpi_num_qcomm == 2
     assert abs(p.ecut_for_eps - 3.0) < 1e-15 and abs(p.max_excitation_energy - 50.0) < 1e-15
     assert q == [1, 2, 5]
