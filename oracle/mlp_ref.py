@@ -1,7 +1,8 @@
 """Test infrastructure: a numpy restatement of the band-tail MLP's arithmetic.
 
 The band-tail network has no counterpart in the reference (it is an extension
-of the reference's full band sum, which stays its target and judge), so this
+of the reference's full band sum, which stays its target and its error
+measure), so this
 module restates the library's own definition (respackdev_gb300/csrc/rp_mlp.cu)
 in float64 numpy, to check the GPU forward pass, loss and gradients:
 

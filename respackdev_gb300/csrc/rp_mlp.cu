@@ -5,7 +5,7 @@
 // per |q+G| shell, from features of the truncated-band chi0 and the band
 // energies (respackdev_gb300/tail.py builds the features and applies the
 // correction).  The reference has no counterpart: the full band sum is both the
-// training target and the judge of the network's error.
+// training target and the measure of the network's error.
 //
 // Weights live as an FP32 master copy (Adam updates it) and a BF16 copy that
 // the forward and backward passes read; every product accumulates in FP32.

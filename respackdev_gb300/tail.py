@@ -3,8 +3,8 @@
 chi0 summed over the bands up to a truncation misses the contribution of the
 bands above it.  Per q, frequency and |q+G| shell, a network predicts that
 tail on the diagonal of chi0 from features of the truncated chi0 and of the
-band energies; the full band sum generates the training targets and judges the
-error (tests/test_gpu_tail.py).  The network's training and inference run in
+band energies; the full band sum generates the training targets and measures
+the error (tests/test_gpu_tail.py).  The network's training and inference run in
 the library (rp_mlp_* of include/respack_gb300.h, respackdev_gb300/csrc/rp_mlp.cu);
 this module builds the features and targets and applies the correction.
 

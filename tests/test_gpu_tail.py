@@ -1,7 +1,7 @@
 """The band-tail MLP on the GPU (rp_mlp_* of the C ABI): forward pass, loss
 and gradients against the numpy restatement (oracle/mlp_ref.py), training,
 and the held-out gain of the tail-corrected chi0 over the truncated band sum,
-with the full band sum as the judge."""
+with the full band sum as the measure of the error."""
 from __future__ import annotations
 
 import dataclasses
