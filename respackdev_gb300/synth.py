@@ -551,7 +551,7 @@ CASES = {
     "wan5": SynthSpec(nk=(3, 3, 3), nbands=24, nocc=4, ecut_psi=8.0, seed=25,
                       wan_lo=5, wan_hi=9, nwf=5, wan_sigma=1.1),
     # fcc a=10.26, 4x4x4 k, 40 bands, 16 Ry, E_F mid-gap, target bands 9-11
-    "config1": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
+    "fcc_4k_40b": SynthSpec(nk=(4, 4, 4), nbands=40, nocc=8, ecut_psi=16.0, seed=1234),
     # the cubic point group on an fcc 4x4x4 mesh: 8 irreducible points unfold
     # to 64 (rotations, time reversal, zone-boundary wraps)
     "tiny_sym": SynthSpec(nk=(4, 4, 4), nbands=10, nocc=4, ecut_psi=6.3, seed=31, wan_lo=5, wan_hi=6,

@@ -48,7 +48,7 @@ def run_params(case: str):
     kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0)
     if case in ("tiny_metal_crpa", "tiny_glide"):
         kw["flg_crpa"] = 1
-    if case == "config1":
+    if case == "fcc_4k_40b":
         kw.update(ecut_for_eps=3.0, flg_crpa=1)
     return kw
 

@@ -24,7 +24,7 @@ def _chi(root, qs, **kw):
 
 @pytest.mark.parametrize("prec", [rp.PREC_FP16X3, rp.PREC_BF16X3, rp.PREC_FP16X2])
 def test_pair_matches_single(case_dir, fresh_copy, prec):
-    root = fresh_copy(case_dir("config1"))
+    root = fresh_copy(case_dir("fcc_4k_40b"))
     one = _chi(root, (1, 2), precision=prec, tc_pair=1, tc_split=1)
     two = _chi(root, (1, 2), precision=prec, tc_pair=2, tc_split=1)
     for a, b in zip(two, one):
@@ -34,7 +34,7 @@ def test_pair_matches_single(case_dir, fresh_copy, prec):
 
 
 def test_pair_with_k_splits(case_dir, fresh_copy):
-    root = fresh_copy(case_dir("config1"))
+    root = fresh_copy(case_dir("fcc_4k_40b"))
     ref = _chi(root, (2, 3), precision=rp.PREC_FP16X3, tc_pair=1, tc_split=1)
     for split in (2, 5):
         got = _chi(root, (2, 3), precision=rp.PREC_FP16X3, tc_pair=2, tc_split=split)
@@ -44,7 +44,7 @@ def test_pair_with_k_splits(case_dir, fresh_copy):
 
 
 def test_pair_ragged_group(case_dir, fresh_copy):
-    roots = [fresh_copy(case_dir(n)) for n in ("config1", "tiny")]
+    roots = [fresh_copy(case_dir(n)) for n in ("fcc_4k_40b", "tiny")]
     probs_of = lambda ctxs: [(ctxs[0], 1), (ctxs[1], 2), (ctxs[0], 3), (ctxs[1], 1)]
     out = {}
     for pair in (1, 2):

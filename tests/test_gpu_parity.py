@@ -101,7 +101,7 @@ def test_bad_input_reports_error(case_dir, fresh_copy):
         rp.Context(root + "/nonexistent", rp.default_params(), EM_TEST)
 
 
-@pytest.mark.parametrize("case,qs", [("tiny", [1, 2, 5]), ("tiny_metal", [1, 3]), ("config1", [1, 2, 7]),
+@pytest.mark.parametrize("case,qs", [("tiny", [1, 2, 5]), ("tiny_metal", [1, 3]), ("fcc_4k_40b", [1, 2, 7]),
                                      ("tiny_glide", [1, 4, 8])])
 @pytest.mark.parametrize("pair64", [0, 1])
 @pytest.mark.parametrize("prec", [rp.PREC_FP16X3, rp.PREC_BF16X3, rp.PREC_FP16X2])

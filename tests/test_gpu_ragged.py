@@ -109,7 +109,7 @@ def test_k_splits_agree_and_tuner_caches(case_dir, fresh_copy):
     word carries the correction products in FP32 (about 2^-31 of chi per
     sub-chunk, so another K partition moves chi by ~1e-9); the tuner measures
     the shape once."""
-    root = fresh_copy(case_dir("config1"))
+    root = fresh_copy(case_dir("fcc_4k_40b"))
     kw = dict(green_func_delt=0.2721, ecut_for_eps=3.0, flg_crpa=1, precision=rp.PREC_FP16X3)
     em = EM_TEST
     res = {}
