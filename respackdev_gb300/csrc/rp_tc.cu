@@ -30,14 +30,17 @@
 // frequency, Re/Im weight, K split) -- of a work list.  A q point is a group of
 // one problem; a ragged batch (several q points of several cells) is one
 // launch over all its problems.  Small problems split K across CTAs, each
-// split into its own slice of the sums, added when chi is assembled; the split
-// of a shape is measured once and cached (tc_begin_q, tune_split).
+// split into its own slice of the sums, added when chi is assembled.  Work
+// items can also run as CTA pairs (tcgen05.mma.cta_group::2 on 2 x 2 tile
+// blocks; see tc_gram_kernel).  The K split and the CTA shape of a problem
+// shape are measured once and cached (tc_begin_q, tune_shape).
 //   warps 0-15  producers (8 rows each): read the FP32 rows of the A operand (prefetched one K
 //               block ahead in registers), multiply by the weights, split into
 //               planes and store them into shared memory in the 128-byte-swizzled
 //               K-major layout the tensor core reads;
 //   warps 16-19 epilogue: drain the FP32 accumulators from tensor memory
-//               (tcgen05.ld) into the float-pair tile in global memory;
+//               (tcgen05.ld) into the float-pair tile in global memory (in a
+//               CTA pair the producer warps help: drain_sub);
 //   warp 20     allocates tensor memory and issues tcgen05.mma (one thread);
 //   warp 21     loader (one thread): bulk-copies (cp.async.bulk) the B operand
 //               planes -- split once per batch by bplanes_kernel and shared by
