@@ -18,8 +18,11 @@
 extern "C" {
 #endif
 
-/* Arithmetic of the chi0 contraction (the rest of the path is fixed:
- * FP64 tetrahedron weights, FP64 eps and its inversion). */
+/* Arithmetic of the path.  RP_PREC_FP64 is FP64 throughout, as the reference.
+ * The split precisions take FP32 pair densities and real-space transforms,
+ * the FP32 tetrahedron series (FP64 closed forms where it does not converge;
+ * tetra_fp64 = 1: everywhere), the tensor-core contraction below, and the
+ * mixed-precision eps inverse (eps_fp64 = 1: FP64); eps is built in FP64. */
 enum rp_precision {
   RP_PREC_FP64 = 0,    /* plain FP64 everywhere (pair densities, contraction)      */
   RP_PREC_FP16X2 = 1,  /* FP32 pair densities; tcgen05 contraction, 2-term FP16
