@@ -357,7 +357,8 @@ def run_gpu(args):
             line = {"metric": METRIC,
                     "value": value, "unit": "s/q-point", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                     "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": False, "scaling": "weak",
-                    "vs_baseline": None, "dtype": "fp16x3-split tensor contraction, f32 pair densities, f64 weights/eps",
+                    "vs_baseline": None, "dtype": "fp16x3-split tensor contraction, f32 pair densities, f32-series weights "
+                             "(f64 closed forms near resonance), f32 Gauss-Jordan + float-pair Newton eps^-1",
                     "data": "synthetic (seeded generator, dir-wfn files)",
                     "config": workload_config(info.ntk, info.ncb, npair_full, ngs[0], info.nen, info.fft_box, timed,
                                               world) | ({} if args.case == "full" else {"workload": WORKLOAD + "_small"}),
